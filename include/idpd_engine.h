@@ -1,0 +1,199 @@
+/*
+ * idpd_engine.h - C ABI of the GB300 engine for the implicit-solvent MDPD
+ * short-range particle step (kohnakagawa/implicit_dpd).
+ *
+ * Plain C: pointers, sizes and status codes only. Every entry point returns an
+ * idpd_status; nothing aborts inside the library. Host arrays belong to the
+ * caller and are copied in and out; device memory belongs to the handle.
+ * Calls on one handle must be serialised by the caller; different handles are
+ * independent. One CUDA stream per handle.
+ *
+ * Each entry point names the reference interface it replaces as
+ * <file>:<line> inside the reference project.
+ */
+#ifndef IDPD_ENGINE_H
+#define IDPD_ENGINE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDPD_ABI_VERSION 1
+
+typedef enum idpd_status {
+  IDPD_OK = 0,
+  IDPD_ERR_INVALID_ARG = 1, /* bad pointer, size, replica index or parameter  */
+  IDPD_ERR_CAPACITY = 2,    /* particle / cell / neighbour capacity exceeded   */
+  IDPD_ERR_CUDA = 3,        /* a CUDA runtime call failed                      */
+  IDPD_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up              */
+  IDPD_ERR_NONFINITE = 5,   /* NaN or Inf found in positions / forces          */
+  IDPD_ERR_STATE = 6,       /* call order violated (e.g. force before upload)  */
+  IDPD_ERR_NO_DEVICE = 7    /* no CUDA device is visible                       */
+} idpd_status;
+
+/* Bead properties (parameter.hpp:208-214). */
+enum { IDPD_HYPHIL = 0, IDPD_HYPHOB = 1, IDPD_SOLVENT = 2, IDPD_PROP_NUM = 3 };
+
+/* Conservative-force form of pass 2.
+ *  MDPD:      CalcForceEpEpDPD default build (nbdf_calculator.hpp:119-123),
+ *             density weight (1-r)^2 with hard cutoff 1 (nbdf_calculator.hpp:38-41).
+ *  PAIRWISE:  the PAIRWISE_DPD build, a = 25 (nbdf_calculator.hpp:114-117).
+ *  WARREN:    Warren's MDPD, A w_C + B (rho_i + rho_j) w_B with w_B = 1 - r/rd and
+ *             density weight 15/(2 pi rd^3) (1 - r/rd)^2. Not in the reference;
+ *             the dissipative and random terms stay the reference's. */
+enum { IDPD_FORM_MDPD = 0, IDPD_FORM_PAIRWISE = 1, IDPD_FORM_WARREN = 2 };
+
+/* Per-system physical parameters. Tables are the reference's static
+ * coefficient tables after CalcInterCoef (parameter.hpp:138-186): cf_r is
+ * already divided by sqrt(dt) and cf_g = cf_r_raw^2 / (2 kT). */
+typedef struct idpd_params {
+  double box[3];
+  double dt;
+  double cf_c[3][3];
+  double cf_g[3][3];
+  double cf_r[3][3];
+  double cf_m[3][3][3];
+  double cf_s;       /* bond coefficient, F = cf_s (1/r - 1/l0) d (parameter.hpp:713-716) */
+  double cf_b;       /* bend coefficient (bdf_calculator.hpp:117-150)                    */
+  double cf_b_rigid; /* bend coefficient of core molecules (bdf_calculator.hpp:77-86)    */
+  double warren_a, warren_b, warren_rd; /* IDPD_FORM_WARREN only */
+  uint32_t seed;     /* CalcForceEpEpDPD::m_seed (nbdf_calculator.hpp:65)   */
+  uint32_t time;     /* Parameter::time of the next force pass (parameter.hpp:261) */
+  int32_t form;      /* IDPD_FORM_* */
+  int32_t reserved;
+} idpd_params;
+
+/* Inputs of Parameter::CalcInterCoef as run_param.txt gives them
+ * (parameter.hpp:74-136; values already rounded through float like std::stof). */
+typedef struct idpd_run_param {
+  double box[3];
+  double dt;
+  double cf_r_upper[6]; /* upper triangle of cf_r, row major (parameter.hpp:29-38, 83-85) */
+  double cf_s, cf_b, cf_b_rigid;
+  double vbb, chi, kappa, rho_co;
+} idpd_run_param;
+
+/* Chemical-reaction parameters of one replica (Parameter members read by
+ * ChemManager, parameter.hpp:230-243; amp_num/max_amp_num parameter.hpp:224,233). */
+typedef struct idpd_chem_params {
+  double p_thresld, eps;
+  double influ_rad, influ_hei, influ_dep, influ_grd;
+  uint32_t amp_num, max_amp_num;
+} idpd_chem_params;
+
+/* Derives idpd_params tables from run_param inputs exactly as
+ * Parameter::CalcInterCoef (parameter.hpp:138-186) with the compile-time
+ * constants of parameter.hpp:189-205. form/seed/time are left at zero. */
+int idpd_derive_params(const idpd_run_param* rp, idpd_params* out);
+
+/* ------------------------------------------------------------------------ */
+/* Engine handle: device-resident state of one or more independent systems
+ * ("replicas") advanced together. Replaces the FDPS ParticleSystem plus the
+ * two Gather trees of src/main.cpp:93-132. */
+
+typedef struct idpd_handle idpd_handle;
+
+typedef struct idpd_config {
+  int32_t n_replicas;      /* >= 1                                              */
+  int32_t capacity;        /* max particles over all replicas (0 = auto at upload) */
+  int32_t device;          /* CUDA device ordinal                               */
+  int32_t flags;           /* IDPD_CFG_*                                        */
+  int32_t sort_period;     /* steps between storage reorders by cell (0 = 100)  */
+  int32_t reserved[3];
+} idpd_config;
+
+#define IDPD_CFG_FP64_PAIRS 0x1 /* plain FP64 pair kernels (baseline arm)       */
+#define IDPD_CFG_TIMING 0x2     /* record per-kernel CUDA events                */
+
+int idpd_create(const idpd_config* cfg, idpd_handle** out);
+int idpd_destroy(idpd_handle* h);
+/* Copies the last error message of the handle (or of the library when h is
+ * NULL) into buf, NUL terminated. */
+int idpd_last_error(const idpd_handle* h, char* buf, size_t len);
+
+/* Parameters of one replica (the Parameter statics + CalcForceEpEpDPD::m_seed). */
+int idpd_set_params(idpd_handle* h, int32_t replica, const idpd_params* p);
+int idpd_get_params(const idpd_handle* h, int32_t replica, idpd_params* p);
+
+/* FPDPD state of one replica, in FPDPD field order (ptcl_class.hpp:29-35):
+ * pos/vel/acc are n x 3 doubles; id/prop/amp_id/unit n uint32 (amp_id and
+ * unit 0xffffffff for solvent). Uploading replica r resets its particle
+ * count to n; replicas are packed in replica order. delta_sumr is reset to 0. */
+int idpd_upload_state(idpd_handle* h, int32_t replica, int32_t n, const double* pos,
+                      const double* vel, const double* acc, const uint32_t* id,
+                      const uint32_t* prop, const uint32_t* amp_id, const uint32_t* unit);
+int idpd_num_particles(const idpd_handle* h, int32_t replica, int32_t* n);
+/* Any pointer may be NULL to skip that field. Rows come back in the order
+ * they were uploaded (new particles from chemistry appended). */
+int idpd_download_state(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc,
+                        uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit);
+/* Derived per-particle fields: density[3] (FPDPD::density), press[3]
+ * (FPDPD::press), nei_cm_pos[2][3] (FPDPD::nei_cm_pos), delta_sumr[3]. */
+int idpd_download_aux(idpd_handle* h, int32_t replica, double* density, double* press,
+                      double* nei_cm_pos, double* delta_sumr);
+
+/* Molecule topology of one replica: ForceBonded ctor (bdf_calculator.hpp:32-88):
+ * glob_topol[amp*4+unit] = particle row, bend coefficient cf_b or cf_b_rigid for
+ * the listed core molecules. Built from the uploaded amp_id/unit fields. */
+int idpd_build_topology(idpd_handle* h, int32_t replica, int32_t n_amp, int32_t n_core,
+                        const uint32_t* core_amp_id);
+
+/* ---- fine-grained passes (all replicas at once) ------------------------- */
+
+/* drift_and_predict (driftkick.hpp:6-27). */
+int idpd_drift(idpd_handle* h);
+/* dens_tree.calcForceAllAndWriteBack(CalcDensity()) (src/main.cpp:173;
+ * nbdf_calculator.hpp:11-60; write-back ptcl_class.hpp:53-57), including the
+ * neighbour centre-of-mass sums. */
+int idpd_density(idpd_handle* h);
+/* force_tree.calcForceAllAndWriteBack(CalcForceEpEpDPD()) (src/main.cpp:174;
+ * nbdf_calculator.hpp:63-145; write-back ptcl_class.hpp:48-51): acc is
+ * overwritten, press written. */
+int idpd_force(idpd_handle* h);
+/* ForceBonded::CalcListedForce (bdf_calculator.hpp:191-220): acc += bond and
+ * bend forces. vir receives 3 doubles per replica (may be NULL). */
+int idpd_bonded(idpd_handle* h, double* vir);
+/* kick (driftkick.hpp:33-40). */
+int idpd_kick(idpd_handle* h);
+/* remove_cmdrift_global (driftkick.hpp:43-54), per replica. */
+int idpd_remove_cmdrift(idpd_handle* h);
+
+/* nsteps iterations of the main loop body of src/main.cpp:166-184 (drift,
+ * density, force, bonded, kick, centre-of-mass drift removal every 100 steps,
+ * time += 1) for every replica, captured once into a CUDA graph and replayed.
+ * Per-particle press and nei_cm_pos are not produced by this path. */
+int idpd_step(idpd_handle* h, int32_t nsteps);
+/* Blocks until the handle's stream is idle; reports device-side errors. */
+int idpd_sync(idpd_handle* h);
+
+/* ---- timing -------------------------------------------------------------- */
+/* Elapsed milliseconds of the last idpd_step call measured with CUDA events
+ * on the handle's stream. */
+int idpd_last_step_ms(const idpd_handle* h, float* ms);
+/* Per-kernel event timing of one un-graphed step (IDPD_CFG_TIMING): names is a
+ * '\n'-separated list, ms one entry per name. */
+int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, int32_t max_k,
+                      int32_t* n_k);
+
+/* ---- Saru (saruprng.hpp:83-445) on the device ----------------------------- */
+/* out[k] = k-th u32() of Saru(s1[i], s2[i], s3[i]) for k < draws, i < n
+ * (row-major n x draws). */
+int idpd_saru_u32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
+                  int32_t draws, uint32_t* out);
+/* FP32 Box-Muller normal of Saru(s1,s2,s3).nrml() as the pair kernel computes it. */
+int idpd_saru_nrml_f32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
+                       float* out);
+
+/* ---- cell list (the FDPS gather replacement) ----------------------------- */
+/* Cell index per particle row and the stable cell-sorted order of the rows
+ * for replica `replica` (grid: floor(box/r_cell) cells per axis, r_cell the
+ * pair cutoff 1.0). perm[k] = row at sorted position k. */
+int idpd_cell_order(idpd_handle* h, int32_t replica, uint32_t* cell_of_row, uint32_t* perm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IDPD_ENGINE_H */
