@@ -1,0 +1,363 @@
+"""Throughput of the short-range particle step on one GB300 (particle-steps/s).
+
+Workload (the ~10^6-bead membrane system the metric is quoted on):
+  membrane_1m - 10 flat bilayers of 1-hydrophilic + 3-hydrophobic chains
+  stacked along z in a periodic 64 x 64 x 48 box, area per lipid 0.333
+  (input_generator.py:69), 246,010 molecules = 984,040 beads; reference MDPD
+  form (chi 30, kappa 100, rho_co 40, vbb 0.1), sigma 3, dt 0.005, bonds
+  cf_s = 50 (k = cf_s / l0 = 100, l0 = 0.5), bend cf_b = 10. Seeded synthetic
+  input (no dataset is involved).
+
+Arms:
+  engine (default)  the FP32-pair / fixed-point engine, one CUDA graph per step;
+                    also reports the plain FP64 pair kernels on the same
+                    workload, the end-to-end rate through the C ABI with pinned
+                    host buffers, the roofline of the force kernel and the CPU
+                    oracle on a bounded sample (cpu_baseline).
+  reference         the reference's CPU algorithm (the C oracle, all host
+                    threads) on a bounded sample of the same workload.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from implicit_dpd_gb300 import configs  # noqa: E402
+
+BOX = np.array([64.0, 64.0, 48.0])
+N_LAYERS = 10
+AREA_PER_LIPID = 0.333
+METRIC = "particle-steps/s on 1 GB300: FP32+batched vs plain FP64 kernel at stated force err"
+# force kernel algorithmic HBM bytes per particle: posf, velf, densf of the
+# particle itself (3 x 16 B) and its fixed-point force (3 x 8 B)
+FORCE_BYTES_PER_PARTICLE = 72
+STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
+KERNELS_PER_STEP = 14          # drift_bin, scan x3, scatter, cell_sort, pack,
+                               # density, force, bonded_kick, cmdrift x3, time
+KERNELS_PER_REORDER = 4        # gather, topology, identity, loc
+
+
+def n_amp_for(box, layers):
+    return layers * int(round(2 * box[0] * box[1] / AREA_PER_LIPID))
+
+
+def workload(box=BOX, layers=N_LAYERS, seed=20250101):
+    n_amp = n_amp_for(box, layers)
+    st = configs.flat_bilayers(box, n_amp, seed=seed, n_layers=layers)
+    rp = configs.run_param(box, dt=0.005, cf_r=3.0, cf_s=50.0, cf_b=10.0, vbb=0.1, chi=30.0,
+                           kappa=100.0, rho_co=40.0)
+    return st, n_amp, rp
+
+
+def workload_desc(n, n_amp):
+    return {
+        "workload": "membrane_1m",
+        "description": ("10 flat bilayers of 1H+3T chains stacked in a periodic 64x64x48 box, "
+                        "reference MDPD form (chi 30, kappa 100, rho_co 40, vbb 0.1), sigma 3, "
+                        "dt 0.005, cf_s 50, cf_b 10"),
+        "n_particles": int(n),
+        "n_molecules": int(n_amp),
+        "l2": "inputs larger than L2 (device state ~200 MB per replica)",
+    }
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    def __init__(self, world):
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.td.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("[N/A]", "N/A") else 0.0,
+                             f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per force-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "force_membrane_1m.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(min_seconds=10.0, max_steps=50):
+    """The C oracle (the reference's CPU algorithm, FP64) on one bilayer period
+    of the workload: a 64 x 64 x 4.8 slab, 98,404 beads, every host thread."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+
+    box = np.array([BOX[0], BOX[1], BOX[2] / N_LAYERS])
+    st, n_amp, rp = workload(box=box, layers=1, seed=7)
+    p = O.derive_params(rp)
+    p.seed, p.time = 1, 1
+    st["topol"], st["cf_bend"] = O.build_topology(st["amp_id"], st["unit"], n_amp, [], p.cf_b,
+                                                  p.cf_b_rigid)
+    threads = os.cpu_count() or 1
+    O.md_step(p, st, nthreads=threads)  # warm-up
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps:
+        O.md_step(p, st, nthreads=threads)
+        steps += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    n = len(st["pos"])
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} MD steps (drift, density, force, bonded, kick) of a 64x64x4.8 slab "
+                      f"holding one bilayer of the workload ({n} beads), FP64 C oracle, OpenMP"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+
+    box = np.array([BOX[0], BOX[1], BOX[2] / N_LAYERS])
+    st, n_amp, rp = workload(box=box, layers=1, seed=7)
+    p = O.derive_params(rp)
+    p.seed, p.time = 1, 1
+    st["topol"], st["cf_bend"] = O.build_topology(st["amp_id"], st["unit"], n_amp, [], p.cf_b,
+                                                  p.cf_b_rigid)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.md_step(p, st, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.md_step(p, st, nthreads=threads)
+    dt = time.perf_counter() - t0
+    n = len(st["pos"])
+    value = n * args.steps / dt
+    sample = (f"each step one MD step (drift, density, force, bonded, kick) of a 64x64x4.8 slab "
+              f"holding one bilayer of membrane_1m ({n} beads), FP64 C oracle of the reference "
+              f"algorithm, OpenMP")
+    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": workload_desc(n, n_amp), "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def make_engine(st, n_amp, rp, flags=0):
+    from implicit_dpd_gb300.engine import Engine, derive_params
+
+    p = derive_params(rp)
+    p.seed, p.time = 12345, 1
+    e = Engine(flags=flags, sort_period=100)
+    e.set_params(p)
+    e.upload(st)
+    e.build_topology(n_amp)
+    return e
+
+
+def pinned(shape):
+    import torch
+
+    t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    return t, t.numpy()
+
+
+def run_engine(args, rank, world, local_rank):
+    from implicit_dpd_gb300.abi import CFG_FP64_PAIRS
+
+    dist = Dist(world)
+    st, n_amp, rp = workload()
+    n = len(st["pos"])
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    e = make_engine(st, n_amp, rp)
+    e.step(max(args.warmup, 3))
+    dist.barrier()
+    e.sync()
+    clk = Clocks(local_rank)
+    clk.start()
+    e.step(args.steps)  # CUDA events around the steps on the engine's stream
+    ms = e.last_step_ms()
+    clocks = clk.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = n * args.steps * world / (ms_max * 1e-3)
+
+    # per-kernel CUDA-event times of un-graphed steps (dominant kernel = force)
+    prof = [e.profile_step() for _ in range(5)]
+    force_ms = statistics.median(p_["force"] for p_ in prof)
+    kernel_ms = {k: statistics.median(p_[k] for p_ in prof) for k in prof[0]}
+    peak, peak_kind = measured_peaks()
+    achieved = FORCE_BYTES_PER_PARTICLE * n / (force_ms * 1e-3) / 1e9
+    traffic = profiled_traffic()
+    roofline = {"kernel": "k_force_f32", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_kind} copy bandwidth", "force_ms": force_ms,
+                "bytes_per_particle": FORCE_BYTES_PER_PARTICLE,
+                "note": "the force pass is bound by CUDA-core issue (Saru + transcendentals "
+                        "per pair), not by HBM"}
+    step_gbs = STEP_BYTES_PER_PARTICLE * n / (ms_max / args.steps * 1e-3) / 1e9
+
+    # plain FP64 pair kernels on the same workload (the baseline of the metric)
+    fp64 = None
+    if not args.no_fp64:
+        e64 = make_engine(st, n_amp, rp, flags=CFG_FP64_PAIRS)
+        e64.step(1)
+        k64 = max(2, min(args.steps, 10))
+        e64.step(k64)
+        ms64 = e64.last_step_ms()
+        v64 = n * k64 / (ms64 * 1e-3)
+        fp64 = {"value": v64, "unit": "particle-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
+                "speedup_fp32_over_fp64": value / world / v64}
+        e64.close()
+
+    # end to end through the C ABI: host pinned pos/vel/acc in, one step, out
+    e2e = None
+    if not args.no_e2e:
+        tp, pos = pinned((n, 3))
+        tv, vel = pinned((n, 3))
+        ta, acc = pinned((n, 3))
+        e.download_dynamics(pos, vel, acc)
+        k2 = max(3, min(args.steps, 50))
+        e.sync()
+        t0 = time.perf_counter()
+        for _ in range(k2):
+            e.set_dynamics(pos, vel, acc)
+            e.step(1)
+            e.download_dynamics(pos, vel, acc)
+        t2 = time.perf_counter() - t0
+        e2e = {"value": n * k2 * world / dist.max(t2), "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": k2,
+               "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state per step"}
+
+    cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
+    n_reorders = args.steps // 100
+    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+           "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic", "config": dict(workload_desc(n, n_amp),
+                                               parallelism=f"replicas{world}" if world > 1 else "single"),
+           "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
+           "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
+           "gpu_launches": args.steps * KERNELS_PER_STEP + n_reorders * KERNELS_PER_REORDER,
+           "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    e.close()
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_engine(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

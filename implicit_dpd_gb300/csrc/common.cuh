@@ -1,0 +1,139 @@
+// Shared device-side definitions of the GB300 engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace idpd {
+
+// Compile-time constants of the reference model (parameter.hpp:189-205).
+constexpr int kAllUnit = 4;       // head_unit + tail_unit
+constexpr double kBondLeng = 0.5; // bond_leng (ibond = 2)
+constexpr float kArc = 0.9f;      // arc
+constexpr double kArcD = 0.9;
+constexpr uint32_t kCmCorr = 100; // cm_corr
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Conservative-force forms (IDPD_FORM_* of include/idpd_engine.h).
+constexpr int IDPD_FORM_MDPD_K = 0;
+constexpr int IDPD_FORM_PAIRWISE_K = 1;
+constexpr int IDPD_FORM_WARREN_K = 2;
+
+// Fixed-point scales of the order-independent accumulators.
+constexpr double kForceScale = 4294967296.0;         // 2^32 per unit force
+constexpr double kForceUnscale = 1.0 / 4294967296.0;
+constexpr float kForceScaleF = 4294967296.0f;
+constexpr double kDensScale = 1099511627776.0;        // 2^40 per unit density
+constexpr float kDensScaleF = 1099511627776.0f;
+constexpr double kDensUnscale = 1.0 / 1099511627776.0;
+constexpr double kPosScale = 1099511627776.0;         // 2^40: COM sums, delta_sumr
+constexpr float kPosScaleF = 1099511627776.0f;
+
+// FP32 pair-set decisions within this band of a cutoff are re-taken in FP64
+// from the FP64 positions, exactly as the reference's FP64 test. The bound on
+// the FP32 error of dr^2 for |d| <= 1.5 cells is below 2e-6.
+constexpr float kGuard = 8.0e-6f;
+
+// Per-replica parameters on the device. Pair tables are FP32 copies of the
+// reference's FP64 tables; geometry is kept in FP64 for the exact paths.
+struct RepDev {
+  double box[3];
+  double ibox[3];    // 1 / box (Parameter::ibox_leng)
+  double inv_cs[3];  // cells per unit length (nc / box)
+  double cs[3];      // cell side (box / nc)
+  float cs_f[3];
+  int nc[3];
+  int cell_off;      // first global cell of the replica
+  int ncell;
+  int row_off;       // first row (storage and sorted) of the replica
+  int n;             // rows in use
+  int blk_off;       // first block of the replica in row-block launches
+  int nblk;
+  double dt;
+  float cf_c[9], cf_g[9], cf_r[9], cf_m[27];
+  float wa, wb, wrd, winv_rd, wnorm;  // Warren form
+  float cf_s;
+  uint32_t seed;
+  int form;
+  int n_amp;         // molecules of the replica
+  int amp_off;       // first molecule slot in the global topology
+};
+
+// Row-block launch: block b covers rows [blk_row[b], blk_row[b] + blockDim)
+// of replica blk_rep[b] (rows beyond the replica's end are idle).
+struct BlockMap {
+  const int* rep;
+  const int* row;
+};
+
+__device__ __forceinline__ int sar(int x, int s) { return x >> s; }
+
+// ---------------------------------------------------------------- Saru
+// Saru(seed1, seed2, seed3) and u32() (saruprng.hpp:239-255, 322-333); the
+// constants are the generator's definition and must match bit for bit.
+struct Saru {
+  uint32_t lcg, weyl;
+  __device__ __forceinline__ Saru(uint32_t a, uint32_t b, uint32_t c) {
+    c ^= (a << 7) ^ (b >> 6);
+    b += (a >> 4) ^ (c >> 15);
+    a ^= (b << 9) + (c << 8);
+    c ^= 0xA5366B4Du * ((b >> 11) ^ (a << 1));
+    b += 0x72BE1579u * ((a << 4) ^ (c >> 16));
+    a ^= 0x3F38A6EDu * ((c >> 5) ^ (uint32_t)((int)b >> 22));
+    b += a * c;
+    a += c ^ (b >> 2);
+    b ^= (uint32_t)((int)b >> 17);
+    lcg = 0x79dedea3u * (a ^ (uint32_t)((int)a >> 14));
+    weyl = (lcg + b) ^ (uint32_t)((int)lcg >> 8);
+    lcg = lcg + (weyl * (weyl ^ 0xdddf97f5u));
+    weyl = 0xABCB96F7u + (weyl >> 1);
+  }
+  __device__ __forceinline__ uint32_t next() {
+    lcg = 0x4beb5d59u * lcg + 0x2600e1f7u;
+    weyl = weyl + 0x8009d14bu + ((uint32_t)((int)weyl >> 31) & 0xda879addu);
+    const uint32_t v = (lcg ^ (lcg >> 26)) + weyl;
+    return (v ^ (v >> 20)) * 0x6957f5a7u;
+  }
+};
+
+// Normal deviate of Saru::nrml() (saruprng.hpp:442-445) in FP32:
+// sqrt(-2 ln u1) cos(2 pi u2) with u = (2 (draw >> 1) + 1) / 2^32.
+// -ln u1 is taken from the exact complement 1 - u1 through log1p when u1 >=
+// 1/2, and the cosine argument is folded to (0, 1) in integers, so neither
+// factor loses relative accuracy at the ends of the interval.
+__device__ __forceinline__ float saru_nrml_f32(Saru& s) {
+  const uint32_t d1 = s.next();
+  const uint32_t d2 = s.next();
+  const uint32_t m1 = d1 | 1u;  // 2 (d1 >> 1) + 1
+  float nlog;
+  if (m1 < 0x80000000u) {
+    nlog = -logf(__uint2float_rn(m1) * 2.3283064365386963e-10f);  // 2^-32
+  } else {
+    const uint32_t c = 0u - m1;  // 2^32 - m1: exact complement, odd
+    nlog = -log1pf(-(__uint2float_rn(c) * 2.3283064365386963e-10f));
+  }
+  uint32_t m2 = d2 | 1u;
+  if (m2 > 0x80000000u) m2 = 0u - m2;  // cos(pi x) = cos(pi (2 - x))
+  const float cs = cospif(__uint2float_rn(m2) * 4.6566128730773926e-10f);  // 2^-31
+  return sqrtf(2.0f * nlog) * cs;
+}
+
+// FP64 normal exactly as the reference computes it (plain FP64 arm).
+__device__ __forceinline__ double saru_nrml_f64(Saru& s) {
+  const double u1 = ((double)(int)(s.next() >> 1) + 0.5) * (1.0 / 2147483648.0);
+  const double u2 = ((double)(int)(s.next() >> 1) + 0.5) * (1.0 / 2147483648.0);
+  return sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
+}
+
+// Float with bits reinterpreted as a uint32 payload (prop / id in .w lanes).
+__device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+
+// Cell coordinates of a replica-local cell index (x fastest).
+__device__ __forceinline__ void cell_xyz(int lc, const int* nc, int& cx, int& cy, int& cz) {
+  cx = lc % nc[0];
+  const int t = lc / nc[0];
+  cy = t % nc[1];
+  cz = t / nc[1];
+}
+
+}  // namespace idpd

@@ -1,0 +1,1034 @@
+// Host side of the C ABI in include/idpd_engine.h: handle life cycle,
+// replica layout, uploads and downloads, the per-step launch sequence and its
+// CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "idpd_engine.h"
+#include "state.cuh"
+
+using namespace idpd;
+
+namespace {
+
+std::string g_lib_err;
+
+struct Staged {  // one replica's rows as uploaded (upload order)
+  std::vector<double> pos, vel, acc;
+  std::vector<uint32_t> id, prop, amp_id, unit;
+  std::vector<uint32_t> topol;  // local rows, 4 per molecule
+  std::vector<float> cf_bend;
+  int n_amp = 0;
+};
+
+}  // namespace
+
+struct idpd_handle {
+  int device = 0;
+  int flags = 0;
+  int sort_period = 100;
+  int R = 1;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<idpd_params> params;
+  std::vector<char> params_set;
+  std::vector<Staged> staged;
+  std::vector<int> n;       // rows per replica
+  std::vector<int> n_amp;   // molecules per replica
+  std::vector<RepDev> reps_h;
+  bool layout_dirty = true;   // device arrays must be rebuilt from staging
+  bool reps_dirty = true;     // RepDev table must be re-uploaded
+  bool on_device = false;     // device arrays hold the current state
+  bool density_valid = false;
+  int cap = 0;                // allocated rows
+  int ncell_cap = 0, ncell_tot = 0;
+  int nblk = 0, nblk_cap = 0;
+  int n_tot = 0, n_amp_tot = 0, n_amp_cap = 0;
+  DevState d{}, o{};          // state and reorder scratch
+  std::vector<void*> allocs;
+  // aux buffers of the fine-grained API
+  double *press64 = nullptr, *cm64 = nullptr, *vir_part = nullptr;
+  double* xfer = nullptr;     // device staging of the per-step exchange
+  uint32_t* cm_cnt = nullptr;
+  int* amp_rep = nullptr;
+  // graph
+  cudaGraphExec_t graph = nullptr;
+  int steps_since_sort = 0;
+  float last_ms = 0.f;
+  PairTuning tune{48, kRowBlock};
+  std::string err;
+};
+
+namespace {
+
+int fail(idpd_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h)
+    h->err = buf;
+  else
+    g_lib_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(h, IDPD_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));      \
+  } while (0)
+
+template <class T>
+int dalloc(idpd_handle* h, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "cudaMalloc(%zu B): %s", count * sizeof(T),
+                                    cudaGetErrorString(e));
+  h->allocs.push_back((void*)*p);
+  return IDPD_OK;
+}
+
+void free_all(idpd_handle* h) {
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  for (void* p : h->allocs) cudaFree(p);
+  h->allocs.clear();
+  h->d = DevState{};
+  h->o = DevState{};
+  h->press64 = h->cm64 = h->vir_part = nullptr;
+  h->xfer = nullptr;
+  h->cm_cnt = nullptr;
+  h->amp_rep = nullptr;
+  h->cap = h->ncell_cap = h->nblk_cap = h->n_amp_cap = 0;
+}
+
+void invalidate_graph(idpd_handle* h) {
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+}
+
+int check_params(idpd_handle* h, const idpd_params* p) {
+  for (int k = 0; k < 3; k++) {
+    if (!(std::isfinite(p->box[k]) && p->box[k] >= 3.0))
+      return fail(h, IDPD_ERR_INVALID_ARG, "box[%d] = %g: every box side must be >= 3 (3 cells of the cutoff 1)", k, p->box[k]);
+  }
+  if (!(std::isfinite(p->dt) && p->dt > 0.0)) return fail(h, IDPD_ERR_INVALID_ARG, "dt must be > 0");
+  if (p->form < IDPD_FORM_MDPD || p->form > IDPD_FORM_WARREN)
+    return fail(h, IDPD_ERR_INVALID_ARG, "unknown form %d", p->form);
+  if (p->form == IDPD_FORM_WARREN && !(p->warren_rd > 0.0 && p->warren_rd <= 1.0))
+    return fail(h, IDPD_ERR_INVALID_ARG, "warren_rd must be in (0, 1]");
+  const double* tabs[4] = {&p->cf_c[0][0], &p->cf_g[0][0], &p->cf_r[0][0], &p->cf_m[0][0][0]};
+  const int sz[4] = {9, 9, 9, 27};
+  for (int t = 0; t < 4; t++)
+    for (int k = 0; k < sz[t]; k++)
+      if (!std::isfinite(tabs[t][k])) return fail(h, IDPD_ERR_NONFINITE, "non-finite coefficient table entry");
+  return IDPD_OK;
+}
+
+void fill_repdev(RepDev& R, const idpd_params& p) {
+  for (int k = 0; k < 3; k++) {
+    R.box[k] = p.box[k];
+    R.ibox[k] = 1.0 / p.box[k];
+    R.nc[k] = (int)(p.box[k] / 1.0);
+    R.inv_cs[k] = (double)R.nc[k] / p.box[k];
+    R.cs[k] = p.box[k] / (double)R.nc[k];
+    R.cs_f[k] = (float)R.cs[k];
+  }
+  R.ncell = R.nc[0] * R.nc[1] * R.nc[2];
+  R.dt = p.dt;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      R.cf_c[3 * i + j] = (float)p.cf_c[i][j];
+      R.cf_g[3 * i + j] = (float)p.cf_g[i][j];
+      R.cf_r[3 * i + j] = (float)p.cf_r[i][j];
+      for (int k = 0; k < 3; k++) R.cf_m[9 * i + 3 * j + k] = (float)p.cf_m[i][j][k];
+    }
+  R.wa = (float)p.warren_a;
+  R.wb = (float)p.warren_b;
+  R.wrd = p.form == IDPD_FORM_WARREN ? (float)p.warren_rd : 1.0f;
+  R.winv_rd = 1.0f / R.wrd;
+  const double rd = p.form == IDPD_FORM_WARREN ? p.warren_rd : 1.0;
+  R.wnorm = (float)(15.0 / (2.0 * 3.14159265358979323846 * rd * rd * rd));
+  R.cf_s = (float)p.cf_s;
+  R.seed = p.seed;
+  R.form = p.form;
+}
+
+// Allocates (or grows) every device array for the current layout.
+int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
+  const bool grow = rows > h->cap || ncell > h->ncell_cap || nblk > h->nblk_cap ||
+                    namp > h->n_amp_cap;
+  if (!grow && h->d.px) return IDPD_OK;
+  free_all(h);
+  const int cap = std::max(rows, 1);
+  const int cc = std::max(ncell, 1);
+  const int bc = std::max(nblk, 1);
+  const int ac = std::max(namp, 1);
+  DevState& d = h->d;
+  DevState& o = h->o;
+  int rc = IDPD_OK;
+#define AL(ptr, cnt) \
+  if ((rc = dalloc(h, &(ptr), (cnt))) != IDPD_OK) return rc
+  for (DevState* s : {&d, &o}) {
+    AL(s->px, cap); AL(s->py, cap); AL(s->pz, cap);
+    AL(s->vx, cap); AL(s->vy, cap); AL(s->vz, cap);
+    AL(s->ax, cap); AL(s->ay, cap); AL(s->az, cap);
+    AL(s->dsx, cap); AL(s->dsy, cap); AL(s->dsz, cap);
+    AL(s->id, cap); AL(s->prop, cap); AL(s->amp_id, cap); AL(s->unit, cap);
+    AL(s->orig, cap); AL(s->key, cap);
+  }
+  AL(d.loc, cap);
+  AL(h->xfer, 9 * (size_t)cap);
+  AL(d.slot, cap);
+  AL(d.cell_cnt, cc);
+  AL(d.cell_start, cc + 1);
+  AL(d.scan_part, (cc + 4095) / 4096 + 1);
+  AL(d.perm, cap); AL(d.rank, cap); AL(d.scell, cap);
+  AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap);
+  AL(d.fqx, cap); AL(d.fqy, cap); AL(d.fqz, cap);
+  AL(d.topol, 4 * ac);
+  AL(d.cf_bend, ac);
+  AL(d.reps, h->R);
+  AL(d.rep_time, h->R);
+  AL(d.blk_rep, bc);
+  AL(d.blk_row, bc);
+  AL(d.blk_part, 3 * bc);
+  AL(d.rep_mean, 3 * h->R);
+  AL(d.err, 1);
+  AL(h->amp_rep, ac);
+  if (h->flags & IDPD_CFG_FP64_PAIRS) { AL(d.dens64, 3 * (size_t)cap); }
+#undef AL
+  d.pqx = d.pqy = d.pqz = nullptr;
+  d.dqx = d.dqy = d.dqz = nullptr;
+  CK(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * cc, h->st));
+  CK(cudaMemsetAsync(d.err, 0, sizeof(int), h->st));
+  h->cap = cap;
+  h->ncell_cap = cc;
+  h->nblk_cap = bc;
+  h->n_amp_cap = ac;
+  return IDPD_OK;
+}
+
+int ensure_aux(idpd_handle* h) {
+  if (h->press64) return IDPD_OK;
+  int rc;
+  DevState& d = h->d;
+  if ((rc = dalloc(h, &d.pqx, h->cap)) || (rc = dalloc(h, &d.pqy, h->cap)) ||
+      (rc = dalloc(h, &d.pqz, h->cap)) || (rc = dalloc(h, &d.dqx, h->cap)) ||
+      (rc = dalloc(h, &d.dqy, h->cap)) || (rc = dalloc(h, &d.dqz, h->cap)) ||
+      (rc = dalloc(h, &h->press64, 3 * (size_t)h->cap)) ||
+      (rc = dalloc(h, &h->cm64, 6 * (size_t)h->cap)) ||
+      (rc = dalloc(h, &h->cm_cnt, 2 * (size_t)h->cap)) ||
+      (rc = dalloc(h, &h->vir_part, 3 * (size_t)h->n_amp_cap)))
+    return rc;
+  invalidate_graph(h);  // DevState changed (aux pointers)
+  return IDPD_OK;
+}
+
+// Pulls the device state of every replica back into the staging buffers
+// (upload order) so that the layout can be rebuilt.
+int pull_to_staging(idpd_handle* h);
+
+// Builds the layout from the staging buffers and uploads everything.
+int commit(idpd_handle* h) {
+  if (!h->layout_dirty && !h->reps_dirty) return IDPD_OK;
+  for (int r = 0; r < h->R; r++)
+    if (!h->params_set[r]) return fail(h, IDPD_ERR_STATE, "replica %d has no parameters", r);
+  if (h->layout_dirty) {
+    invalidate_graph(h);
+    h->reps_h.assign(h->R, RepDev{});
+    int row = 0, cell = 0, blk = 0, amp = 0;
+    std::vector<int> blk_rep, blk_row;
+    for (int r = 0; r < h->R; r++) {
+      RepDev& R = h->reps_h[r];
+      fill_repdev(R, h->params[r]);
+      R.row_off = row;
+      R.n = h->n[r];
+      R.cell_off = cell;
+      R.blk_off = blk;
+      R.nblk = (R.n + kRowBlock - 1) / kRowBlock;
+      R.n_amp = h->staged[r].n_amp;
+      R.amp_off = amp;
+      for (int b = 0; b < R.nblk; b++) {
+        blk_rep.push_back(r);
+        blk_row.push_back(row + b * kRowBlock);
+      }
+      row += R.n;
+      cell += R.ncell;
+      blk += R.nblk;
+      amp += R.n_amp;
+      if ((long long)row >= (1ll << 27))
+        return fail(h, IDPD_ERR_CAPACITY, "more than 2^27 particles in one handle");
+      if ((long long)cell >= (1ll << 31) - 1) return fail(h, IDPD_ERR_CAPACITY, "too many cells");
+    }
+    h->n_tot = row;
+    h->ncell_tot = cell;
+    h->nblk = blk;
+    h->n_amp_tot = amp;
+    int rc = ensure_capacity(h, row, cell, blk, amp);
+    if (rc) return rc;
+    DevState& d = h->d;
+    CK(cudaMemcpyAsync(d.blk_rep, blk_rep.data(), sizeof(int) * blk, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(d.blk_row, blk_row.data(), sizeof(int) * blk, cudaMemcpyHostToDevice, h->st));
+    // rows: host transposes into SoA staging, one copy per field
+    std::vector<double> buf(9 * (size_t)std::max(row, 1));
+    std::vector<uint32_t> ub(5 * (size_t)std::max(row, 1));
+    std::vector<uint32_t> topol(4 * (size_t)std::max(amp, 1));
+    std::vector<float> cfb(std::max(amp, 1));
+    std::vector<int> amp_rep(std::max(amp, 1));
+    std::vector<uint32_t> time(h->R);
+    for (int r = 0; r < h->R; r++) {
+      const Staged& s = h->staged[r];
+      const RepDev& R = h->reps_h[r];
+      for (int k = 0; k < R.n; k++) {
+        const size_t i = (size_t)R.row_off + k;
+        for (int c = 0; c < 3; c++) {
+          buf[c * (size_t)row + i] = s.pos[3 * (size_t)k + c];
+          buf[(3 + c) * (size_t)row + i] = s.vel[3 * (size_t)k + c];
+          buf[(6 + c) * (size_t)row + i] = s.acc[3 * (size_t)k + c];
+        }
+        ub[i] = s.id[k];
+        ub[row + i] = s.prop[k];
+        ub[2 * (size_t)row + i] = s.amp_id[k];
+        ub[3 * (size_t)row + i] = s.unit[k];
+        ub[4 * (size_t)row + i] = (uint32_t)i;
+      }
+      for (int a = 0; a < R.n_amp; a++) {
+        for (int u = 0; u < 4; u++)
+          topol[4 * (size_t)(R.amp_off + a) + u] = (uint32_t)R.row_off + s.topol[4 * (size_t)a + u];
+        cfb[R.amp_off + a] = s.cf_bend[a];
+        amp_rep[R.amp_off + a] = r;
+      }
+      time[r] = h->params[r].time;
+    }
+    double* dst[9] = {d.px, d.py, d.pz, d.vx, d.vy, d.vz, d.ax, d.ay, d.az};
+    for (int c = 0; c < 9; c++)
+      CK(cudaMemcpyAsync(dst[c], buf.data() + c * (size_t)row, sizeof(double) * row,
+                         cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(d.loc, ub.data() + 4 * (size_t)row, sizeof(uint32_t) * row,
+                       cudaMemcpyHostToDevice, h->st));
+    uint32_t* udst[5] = {d.id, d.prop, d.amp_id, d.unit, d.orig};
+    for (int c = 0; c < 5; c++)
+      CK(cudaMemcpyAsync(udst[c], ub.data() + c * (size_t)row, sizeof(uint32_t) * row,
+                         cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(d.dsx, 0, sizeof(double) * std::max(row, 1), h->st));
+    CK(cudaMemsetAsync(d.dsy, 0, sizeof(double) * std::max(row, 1), h->st));
+    CK(cudaMemsetAsync(d.dsz, 0, sizeof(double) * std::max(row, 1), h->st));
+    if (amp > 0) {
+      CK(cudaMemcpyAsync(d.topol, topol.data(), sizeof(uint32_t) * 4 * amp, cudaMemcpyHostToDevice, h->st));
+      CK(cudaMemcpyAsync(d.cf_bend, cfb.data(), sizeof(float) * amp, cudaMemcpyHostToDevice, h->st));
+      CK(cudaMemcpyAsync(h->amp_rep, amp_rep.data(), sizeof(int) * amp, cudaMemcpyHostToDevice, h->st));
+    }
+    CK(cudaMemcpyAsync(d.rep_time, time.data(), sizeof(uint32_t) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->layout_dirty = false;
+    h->reps_dirty = true;
+    h->on_device = true;
+    h->density_valid = false;
+    h->steps_since_sort = 0;
+  }
+  if (h->reps_dirty) {
+    for (int r = 0; r < h->R; r++) {
+      RepDev& R = h->reps_h[r];
+      const RepDev keep = R;
+      fill_repdev(R, h->params[r]);
+      R.row_off = keep.row_off; R.n = keep.n; R.cell_off = keep.cell_off; R.blk_off = keep.blk_off;
+      R.nblk = keep.nblk; R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
+      if (R.ncell != keep.ncell) return fail(h, IDPD_ERR_STATE, "box change alters the cell grid; re-upload the state");
+    }
+    CK(cudaMemcpyAsync(h->d.reps, h->reps_h.data(), sizeof(RepDev) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->reps_dirty = false;
+  }
+  return IDPD_OK;
+}
+
+int check_device_error(idpd_handle* h) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (e == 0) return IDPD_OK;
+  CK(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  switch (e) {
+    case kErrNonFinite: return fail(h, IDPD_ERR_NONFINITE, "non-finite pair force");
+    case kErrComBox: return fail(h, IDPD_ERR_INVALID_ARG, "neighbour centre of mass needs >= 5 cells per axis (box >= 5)");
+    default: return fail(h, IDPD_ERR_STATE, "device error code %d", e);
+  }
+}
+
+// Cell list over the current positions (no drift).
+void enqueue_cells(idpd_handle* h, bool drift) {
+  launch_drift_bin(h->d, h->nblk, drift, h->st);
+  launch_scan(h->d, h->ncell_tot, h->n_tot, h->st);
+  launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
+}
+
+void enqueue_step(idpd_handle* h) {
+  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  DevState d = h->d;  // the step writes no fine-grained side outputs
+  d.dqx = d.dqy = d.dqz = nullptr;
+  launch_drift_bin(d, h->nblk, true, h->st);
+  launch_scan(d, h->ncell_tot, h->n_tot, h->st);
+  launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
+  launch_density(d, h->nblk, fp64, h->st);
+  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
+  launch_bonded_kick(d, h->nblk, true, h->st);
+  launch_cmdrift(d, h->nblk, h->R, false, h->st);
+  launch_time_advance(d, h->R, h->st);
+}
+
+int enqueue_reorder(idpd_handle* h) {
+  launch_reorder(h->d, h->o, h->nblk, 4 * h->n_amp_tot, h->st);
+  const size_t n = (size_t)h->n_tot;
+  DevState& d = h->d;
+  DevState& o = h->o;
+  double* dd[12] = {d.px, d.py, d.pz, d.vx, d.vy, d.vz, d.ax, d.ay, d.az, d.dsx, d.dsy, d.dsz};
+  double* od[12] = {o.px, o.py, o.pz, o.vx, o.vy, o.vz, o.ax, o.ay, o.az, o.dsx, o.dsy, o.dsz};
+  for (int k = 0; k < 12; k++)
+    CK(cudaMemcpyAsync(dd[k], od[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+  uint32_t* du[6] = {d.id, d.prop, d.amp_id, d.unit, d.orig, d.key};
+  uint32_t* ou[6] = {o.id, o.prop, o.amp_id, o.unit, o.orig, o.key};
+  for (int k = 0; k < 6; k++)
+    CK(cudaMemcpyAsync(du[k], ou[k], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, h->st));
+  launch_update_loc(h->d, h->nblk, h->st);
+  return IDPD_OK;
+}
+
+int pull_to_staging(idpd_handle* h) {
+  if (!h->on_device) return IDPD_OK;
+  for (int r = 0; r < h->R; r++) {
+    Staged& s = h->staged[r];
+    const int n = h->n[r];
+    s.pos.resize(3 * (size_t)n);
+    s.vel.resize(3 * (size_t)n);
+    s.acc.resize(3 * (size_t)n);
+    s.id.resize(n); s.prop.resize(n); s.amp_id.resize(n); s.unit.resize(n);
+    int rc = idpd_download_state(h, r, s.pos.data(), s.vel.data(), s.acc.data(), s.id.data(),
+                                 s.prop.data(), s.amp_id.data(), s.unit.data());
+    if (rc) return rc;
+  }
+  return IDPD_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+
+extern "C" {
+
+int idpd_derive_params(const idpd_run_param* rp, idpd_params* out) {
+  if (!rp || !out) return fail(nullptr, IDPD_ERR_INVALID_ARG, "null pointer");
+  // Parameter::CalcInterCoef (parameter.hpp:138-186) with Tempera = 1,
+  // all_unit = 4, Reo = 1.4, arc = 0.9 (parameter.hpp:189-205).
+  std::memset(out, 0, sizeof(*out));
+  const double T = 1.0, reo = 1.4, arc = 0.9;
+  const unsigned all_unit = 4u;
+  double c[3][3], g[3][3], s[3][3], m[3][3][3];
+  c[1][1] = -2.0 * (rp->kappa + 3.0) / rp->rho_co;
+  c[0][0] = c[2][2] = rp->vbb;
+  c[0][1] = c[1][0] = rp->chi / (rp->rho_co) + 0.5 * (c[0][0] + c[1][1]);
+  c[2][1] = c[1][2] = c[0][1];
+  c[2][0] = c[0][2] = c[0][0];
+  const double m0 = 1.5 * (rp->kappa + 2.0) / (rp->rho_co * rp->rho_co);
+  for (auto& a : m)
+    for (auto& b : a)
+      for (double& v : b) v = m0;
+  m[0][0][0] = 0.0;
+  m[2][2][2] = 0.0;
+  int k = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = i; j < 3; j++) s[i][j] = rp->cf_r_upper[k++];
+  for (int i = 0; i < 3; i++)
+    for (int j = i + 1; j < 3; j++) s[j][i] = s[i][j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) g[i][j] = 0.5 * s[i][j] * s[i][j] / T;
+  for (int i = 0; i < 3; i++)
+    for (int j = i + 1; j < 3; j++)
+      if (s[i][j] < 0.0) {
+        g[i][j] = g[j][i] = 2.0 / ((1.0 / g[i][i]) + (1.0 / g[j][j]));
+        s[i][j] = s[j][i] = std::sqrt(2.0 * g[i][j] * T);
+      }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) s[i][j] /= std::sqrt(rp->dt);
+  const double mol_energy = (reo * reo * reo) / (double)(all_unit * all_unit);
+  const double arc5 = arc * arc * arc * arc * arc;
+  const double pi = 3.14159265358979323846;
+  const double w2 = -45.0 / ((arc5 * (2.0 * arc - 3.0) + (3.0 * arc - 2.0)) * pi);
+  const double w3 = 15.0 / pi;
+  const double dum = ((reo * reo * reo * 15.0) / (2.0 * pi * (double)all_unit));
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) c[i][j] *= mol_energy * w2;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      for (int q = 0; q < 3; q++) m[i][j][q] *= mol_energy * (2.0 / 3.0) * w3 * dum;
+  std::memcpy(out->cf_c, c, sizeof(c));
+  std::memcpy(out->cf_g, g, sizeof(g));
+  std::memcpy(out->cf_r, s, sizeof(s));
+  std::memcpy(out->cf_m, m, sizeof(m));
+  out->cf_s = rp->cf_s;
+  out->cf_b = rp->cf_b;
+  out->cf_b_rigid = rp->cf_b_rigid;
+  for (int q = 0; q < 3; q++) out->box[q] = rp->box[q];
+  out->dt = rp->dt;
+  return IDPD_OK;
+}
+
+int idpd_create(const idpd_config* cfg, idpd_handle** out) {
+  if (!cfg || !out) return fail(nullptr, IDPD_ERR_INVALID_ARG, "null pointer");
+  *out = nullptr;
+  if (cfg->n_replicas < 1) return fail(nullptr, IDPD_ERR_INVALID_ARG, "n_replicas must be >= 1");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, IDPD_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  if (cfg->device < 0 || cfg->device >= ndev)
+    return fail(nullptr, IDPD_ERR_INVALID_ARG, "device %d out of range", cfg->device);
+  idpd_handle* h = new idpd_handle();
+  h->device = cfg->device;
+  h->flags = cfg->flags;
+  h->sort_period = cfg->sort_period > 0 ? cfg->sort_period : 100;
+  h->R = cfg->n_replicas;
+  h->params.assign(h->R, idpd_params{});
+  h->params_set.assign(h->R, 0);
+  h->staged.assign(h->R, Staged{});
+  h->n.assign(h->R, 0);
+  h->n_amp.assign(h->R, 0);
+  if (cudaSetDevice(h->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+    delete h;
+    return fail(nullptr, IDPD_ERR_CUDA, "stream / event creation failed");
+  }
+  *out = h;
+  return IDPD_OK;
+}
+
+int idpd_destroy(idpd_handle* h) {
+  if (!h) return IDPD_OK;
+  cudaSetDevice(h->device);
+  if (h->st) cudaStreamSynchronize(h->st);
+  free_all(h);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return IDPD_OK;
+}
+
+int idpd_last_error(const idpd_handle* h, char* buf, size_t len) {
+  if (!buf || len == 0) return IDPD_ERR_INVALID_ARG;
+  const std::string& s = h ? h->err : g_lib_err;
+  std::snprintf(buf, len, "%s", s.c_str());
+  return IDPD_OK;
+}
+
+int idpd_set_params(idpd_handle* h, int32_t r, const idpd_params* p) {
+  if (!h || !p) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
+  if (r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", r);
+  int rc = check_params(h, p);
+  if (rc) return rc;
+  const bool geom_changed = !h->params_set[r] ||
+                            std::memcmp(h->params[r].box, p->box, sizeof(p->box)) != 0;
+  h->params[r] = *p;
+  h->params_set[r] = 1;
+  if (geom_changed && h->on_device) {
+    if ((rc = pull_to_staging(h))) return rc;
+    h->layout_dirty = true;
+  }
+  h->reps_dirty = true;
+  if (h->on_device && !h->layout_dirty) {
+    // time is device-resident: update it directly
+    cudaSetDevice(h->device);
+    CK(cudaMemcpyAsync(h->d.rep_time + r, &p->time, sizeof(uint32_t), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return IDPD_OK;
+}
+
+int idpd_get_params(const idpd_handle* h, int32_t r, idpd_params* p) {
+  if (!h || !p || r < 0 || r >= h->R) return IDPD_ERR_INVALID_ARG;
+  *p = h->params[r];
+  if (h->on_device) {
+    uint32_t t = 0;
+    cudaSetDevice(h->device);
+    if (cudaMemcpy(&t, h->d.rep_time + r, sizeof(uint32_t), cudaMemcpyDeviceToHost) == cudaSuccess)
+      p->time = t;
+  }
+  return IDPD_OK;
+}
+
+int idpd_upload_state(idpd_handle* h, int32_t r, int32_t n, const double* pos, const double* vel,
+                      const double* acc, const uint32_t* id, const uint32_t* prop,
+                      const uint32_t* amp_id, const uint32_t* unit) {
+  if (!h) return fail(nullptr, IDPD_ERR_INVALID_ARG, "null handle");
+  if (r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", r);
+  if (n < 0 || (n > 0 && (!pos || !vel || !id || !prop)))
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad size or null array");
+  if (!h->params_set[r]) return fail(h, IDPD_ERR_STATE, "set the parameters of replica %d first", r);
+  const idpd_params& p = h->params[r];
+  for (int i = 0; i < n; i++) {
+    for (int k = 0; k < 3; k++) {
+      const double x = pos[3 * (size_t)i + k];
+      if (!std::isfinite(x) || !std::isfinite(vel[3 * (size_t)i + k]) ||
+          (acc && !std::isfinite(acc[3 * (size_t)i + k])))
+        return fail(h, IDPD_ERR_NONFINITE, "non-finite value in row %d", i);
+      // CheckParticleConfigIsValid (parameter.hpp:456-462)
+      if (!(x >= 0.0 && x <= p.box[k]))
+        return fail(h, IDPD_ERR_INVALID_ARG, "row %d lies outside the box", i);
+    }
+    if (prop[i] >= IDPD_PROP_NUM) return fail(h, IDPD_ERR_INVALID_ARG, "row %d: prop %u", i, prop[i]);
+  }
+  if (h->on_device && !h->layout_dirty) {
+    // the device holds the newest state of every replica: bring it back
+    // before the layout is rebuilt from the staging buffers
+    int rc = pull_to_staging(h);
+    if (rc) return rc;
+  }
+  Staged& s = h->staged[r];
+  s.pos.assign(pos, pos + 3 * (size_t)n);
+  s.vel.assign(vel, vel + 3 * (size_t)n);
+  if (acc)
+    s.acc.assign(acc, acc + 3 * (size_t)n);
+  else
+    s.acc.assign(3 * (size_t)n, 0.0);
+  s.id.assign(id, id + n);
+  s.prop.assign(prop, prop + n);
+  if (amp_id) s.amp_id.assign(amp_id, amp_id + n); else s.amp_id.assign(n, kNone);
+  if (unit) s.unit.assign(unit, unit + n); else s.unit.assign(n, kNone);
+  s.topol.clear();
+  s.cf_bend.clear();
+  s.n_amp = 0;
+  h->n[r] = n;
+  h->n_amp[r] = 0;
+  h->layout_dirty = true;
+  return IDPD_OK;
+}
+
+int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double* vel,
+                      const double* acc) {
+  if (!h || r < 0 || r >= h->R || !pos || !vel || !acc)
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->on_device || h->layout_dirty) return fail(h, IDPD_ERR_STATE, "upload the state first");
+  cudaSetDevice(h->device);
+  const RepDev& R = h->reps_h[r];
+  const size_t n = (size_t)R.n;
+  if (n == 0) return IDPD_OK;
+  // three strided copies interleave pos/vel/acc into 9 doubles per row
+  const size_t row = 9 * sizeof(double), w = 3 * sizeof(double);
+  CK(cudaMemcpy2DAsync(h->xfer, row, pos, w, w, n, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpy2DAsync(h->xfer + 3, row, vel, w, w, n, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpy2DAsync(h->xfer + 6, row, acc, w, w, n, cudaMemcpyHostToDevice, h->st));
+  launch_set_dynamics(h->d, h->xfer, R.row_off, R.n, R.box[0], R.box[1], R.box[2], h->st);
+  h->density_valid = false;
+  return IDPD_OK;
+}
+
+int idpd_num_particles(const idpd_handle* h, int32_t r, int32_t* n) {
+  if (!h || !n || r < 0 || r >= h->R) return IDPD_ERR_INVALID_ARG;
+  *n = h->n[r];
+  return IDPD_OK;
+}
+
+int idpd_build_topology(idpd_handle* h, int32_t r, int32_t n_amp, int32_t n_core,
+                        const uint32_t* core_amp_id) {
+  if (!h || r < 0 || r >= h->R || n_amp < 0 || n_core < 0 || (n_core > 0 && !core_amp_id))
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (h->on_device && !h->layout_dirty) {
+    int rc = pull_to_staging(h);
+    if (rc) return rc;
+  }
+  Staged& s = h->staged[r];
+  const int n = h->n[r];
+  if ((int)s.amp_id.size() != n) return fail(h, IDPD_ERR_STATE, "upload the state first");
+  // MakeGlobalBondedList (bdf_calculator.hpp:61-88)
+  s.topol.assign(4 * (size_t)n_amp, kNone);
+  long long cnt = 0;
+  for (int i = 0; i < n; i++) {
+    const uint32_t a = s.amp_id[i], u = s.unit[i];
+    if (a != kNone && u != kNone) {
+      if (a >= (uint32_t)n_amp || u >= 4u)
+        return fail(h, IDPD_ERR_INVALID_ARG, "row %d: amp_id %u / unit %u out of range", i, a, u);
+      if (s.topol[4 * (size_t)a + u] != kNone)
+        return fail(h, IDPD_ERR_INVALID_ARG, "molecule %u unit %u appears twice", a, u);
+      s.topol[4 * (size_t)a + u] = (uint32_t)i;
+      cnt++;
+    } else if (s.prop[i] != IDPD_SOLVENT) {
+      return fail(h, IDPD_ERR_INVALID_ARG, "row %d has no molecule but is not solvent", i);
+    }
+  }
+  if (cnt != 4ll * n_amp) return fail(h, IDPD_ERR_INVALID_ARG, "topology incomplete: %lld of %d rows", cnt, 4 * n_amp);
+  s.cf_bend.assign(n_amp, (float)h->params[r].cf_b);
+  for (int k = 0; k < n_core; k++)
+    if (core_amp_id[k] < (uint32_t)n_amp) s.cf_bend[core_amp_id[k]] = (float)h->params[r].cf_b_rigid;
+  s.n_amp = n_amp;
+  h->n_amp[r] = n_amp;
+  h->layout_dirty = true;
+  return IDPD_OK;
+}
+
+int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, double* acc,
+                        uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit) {
+  if (!h || r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->on_device || h->layout_dirty) {
+    const Staged& s = h->staged[r];
+    const int n = h->n[r];
+    if (pos) std::copy(s.pos.begin(), s.pos.begin() + 3 * n, pos);
+    if (vel) std::copy(s.vel.begin(), s.vel.begin() + 3 * n, vel);
+    if (acc) std::copy(s.acc.begin(), s.acc.begin() + 3 * n, acc);
+    if (id) std::copy(s.id.begin(), s.id.begin() + n, id);
+    if (prop) std::copy(s.prop.begin(), s.prop.begin() + n, prop);
+    if (amp_id) std::copy(s.amp_id.begin(), s.amp_id.begin() + n, amp_id);
+    if (unit) std::copy(s.unit.begin(), s.unit.begin() + n, unit);
+    return IDPD_OK;
+  }
+  cudaSetDevice(h->device);
+  const RepDev& R = h->reps_h[r];
+  const int n = R.n;
+  if (n == 0) return IDPD_OK;
+  double* tmp = nullptr;
+  CK(cudaMallocAsync((void**)&tmp, sizeof(double) * 3 * (size_t)n, h->st));
+  const DevState& d = h->d;
+  struct F { const double *x, *y, *z; double* out; } f3[3] = {
+      {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
+  int rc = IDPD_OK;
+  for (auto& f : f3) {
+    if (!f.out) continue;
+    launch_soa_to_aos(f.x, f.y, f.z, d.orig, R.row_off, tmp, n, h->st);
+    cudaError_t e = cudaMemcpyAsync(f.out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
+    if (e != cudaSuccess) rc = fail(h, IDPD_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+  }
+  const uint32_t* uf[4] = {d.id, d.prop, d.amp_id, d.unit};
+  uint32_t* uo[4] = {id, prop, amp_id, unit};
+  std::vector<uint32_t> orig(n), tmpu(n);
+  bool need_u = id || prop || amp_id || unit;
+  if (need_u) {
+    CK(cudaMemcpyAsync(orig.data(), d.orig + R.row_off, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  for (int k = 0; k < 4; k++) {
+    if (!uo[k]) continue;
+    CK(cudaMemcpyAsync(tmpu.data(), uf[k] + R.row_off, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int q = 0; q < n; q++) uo[k][orig[q] - (uint32_t)R.row_off] = tmpu[q];
+  }
+  CK(cudaFreeAsync(tmp, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return rc;
+}
+
+int idpd_download_aux(idpd_handle* h, int32_t r, double* density, double* press, double* nei_cm,
+                      double* delta_sumr) {
+  if (!h || r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->on_device || h->layout_dirty) return fail(h, IDPD_ERR_STATE, "no device state");
+  cudaSetDevice(h->device);
+  const RepDev& R = h->reps_h[r];
+  const int n = R.n;
+  if (n == 0) return IDPD_OK;
+  std::vector<uint32_t> orig(n), perm(n);
+  CK(cudaMemcpyAsync(orig.data(), h->d.orig + R.row_off, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  auto scatter3 = [&](const std::vector<double>& src, double* out, int w) {
+    for (int q = 0; q < n; q++)
+      for (int k = 0; k < w; k++)
+        out[(size_t)w * (orig[q] - (uint32_t)R.row_off) + k] = src[(size_t)w * q + k];
+  };
+  if (density) {
+    if (!h->density_valid || !h->d.dqx) return fail(h, IDPD_ERR_STATE, "run idpd_density first");
+    std::vector<long long> q[3];
+    const long long* src[3] = {h->d.dqx, h->d.dqy, h->d.dqz};
+    CK(cudaMemcpyAsync(perm.data(), h->d.perm + R.row_off, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->st));
+    for (int k = 0; k < 3; k++) {
+      q[k].resize(n);
+      CK(cudaMemcpyAsync(q[k].data(), src[k] + R.row_off, sizeof(long long) * n, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    std::vector<double> byrow(3 * (size_t)n);
+    for (int sidx = 0; sidx < n; sidx++) {
+      const int row = (int)perm[sidx] - R.row_off;
+      for (int k = 0; k < 3; k++) byrow[3 * (size_t)row + k] = (double)q[k][sidx] * kDensUnscale;
+    }
+    scatter3(byrow, density, 3);
+  }
+  if (press) {
+    if (!h->press64) return fail(h, IDPD_ERR_STATE, "run idpd_force first");
+    std::vector<double> b(3 * (size_t)n);
+    CK(cudaMemcpyAsync(b.data(), h->press64 + 3 * (size_t)R.row_off, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    scatter3(b, press, 3);
+  }
+  if (nei_cm) {
+    if (!h->cm64) return fail(h, IDPD_ERR_STATE, "run idpd_density first");
+    std::vector<double> b(6 * (size_t)n);
+    CK(cudaMemcpyAsync(b.data(), h->cm64 + 6 * (size_t)R.row_off, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    scatter3(b, nei_cm, 6);
+  }
+  if (delta_sumr) {
+    std::vector<double> b(3 * (size_t)n), t(n);
+    const double* src[3] = {h->d.dsx, h->d.dsy, h->d.dsz};
+    for (int k = 0; k < 3; k++) {
+      CK(cudaMemcpyAsync(t.data(), src[k] + R.row_off, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (int q = 0; q < n; q++) b[3 * (size_t)q + k] = t[q];
+    }
+    scatter3(b, delta_sumr, 3);
+  }
+  return IDPD_OK;
+}
+
+// ---- fine-grained passes
+
+int idpd_drift(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  launch_drift_bin(h->d, h->nblk, true, h->st);
+  // the arrival slots of this binning are not used: reset the cell counts
+  CK(cudaMemsetAsync(h->d.cell_cnt, 0, sizeof(int) * h->ncell_tot, h->st));
+  h->density_valid = false;
+  return check_device_error(h);
+}
+
+int idpd_density(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  if ((rc = ensure_aux(h))) return rc;
+  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  enqueue_cells(h, false);
+  launch_density(h->d, h->nblk, fp64, h->st);
+  launch_com(h->d, h->nblk, h->cm64, h->cm_cnt, h->st);
+  h->density_valid = true;
+  return check_device_error(h);
+}
+
+int idpd_force(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  if (!h->density_valid) return fail(h, IDPD_ERR_STATE, "idpd_force needs idpd_density on the same positions");
+  if ((rc = ensure_aux(h))) return rc;
+  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  launch_force(h->d, h->nblk, fp64, true, h->tune, h->st);
+  launch_fq_to_acc(h->d, h->nblk, h->press64, h->st);
+  return check_device_error(h);
+}
+
+int idpd_bonded(idpd_handle* h, double* vir) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  if ((rc = ensure_aux(h))) return rc;
+  // chain geometry comes from the packed cell-local copies: rebuild them
+  enqueue_cells(h, false);
+  launch_bonded_fine(h->d, h->n_amp_tot, h->amp_rep, h->vir_part, h->st);
+  if ((rc = check_device_error(h))) return rc;
+  if (vir) {
+    std::vector<double> vp(3 * (size_t)std::max(h->n_amp_tot, 1));
+    if (h->n_amp_tot > 0) {
+      CK(cudaMemcpyAsync(vp.data(), h->vir_part, sizeof(double) * 3 * h->n_amp_tot, cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+    }
+    for (int r = 0; r < h->R; r++) {
+      double v[3] = {0.0, 0.0, 0.0};
+      const RepDev& R = h->reps_h[r];
+      for (int a = 0; a < R.n_amp; a++)
+        for (int k = 0; k < 3; k++) v[k] += vp[3 * (size_t)(R.amp_off + a) + k];
+      for (int k = 0; k < 3; k++) vir[3 * r + k] = v[k];
+    }
+  }
+  return IDPD_OK;
+}
+
+int idpd_kick(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  launch_kick_only(h->d, h->nblk, h->st);
+  return check_device_error(h);
+}
+
+int idpd_remove_cmdrift(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  launch_cmdrift(h->d, h->nblk, h->R, true, h->st);
+  return check_device_error(h);
+}
+
+int idpd_step(idpd_handle* h, int32_t nsteps) {
+  if (!h || nsteps < 0) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
+  if (!h->graph) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(h);
+    CK(cudaStreamEndCapture(h->st, &g));
+    cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(h->ev0, h->st));
+  for (int k = 0; k < nsteps; k++) {
+    CK(cudaGraphLaunch(h->graph, h->st));
+    if (++h->steps_since_sort >= h->sort_period) {
+      if ((rc = enqueue_reorder(h))) return rc;
+      h->steps_since_sort = 0;
+    }
+  }
+  CK(cudaEventRecord(h->ev1, h->st));
+  CK(cudaEventSynchronize(h->ev1));
+  CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->density_valid = false;
+  return check_device_error(h);
+}
+
+int idpd_sync(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaStreamSynchronize(h->st));
+  return check_device_error(h);
+}
+
+int idpd_last_step_ms(const idpd_handle* h, float* ms) {
+  if (!h || !ms) return IDPD_ERR_INVALID_ARG;
+  *ms = h->last_ms;
+  return IDPD_OK;
+}
+
+int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, int32_t max_k,
+                      int32_t* n_k) {
+  if (!h || !names || !ms || !n_k) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  std::vector<cudaEvent_t> ev(9);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  const char* nm[8] = {"drift_bin", "scan", "scatter_sort_pack", "density", "force",
+                       "bonded_kick", "cmdrift", "time"};
+  CK(cudaEventRecord(ev[0], h->st));
+  launch_drift_bin(h->d, h->nblk, true, h->st);
+  CK(cudaEventRecord(ev[1], h->st));
+  launch_scan(h->d, h->ncell_tot, h->n_tot, h->st);
+  CK(cudaEventRecord(ev[2], h->st));
+  launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
+  CK(cudaEventRecord(ev[3], h->st));
+  launch_density(h->d, h->nblk, fp64, h->st);
+  CK(cudaEventRecord(ev[4], h->st));
+  launch_force(h->d, h->nblk, fp64, false, h->tune, h->st);
+  CK(cudaEventRecord(ev[5], h->st));
+  launch_bonded_kick(h->d, h->nblk, true, h->st);
+  CK(cudaEventRecord(ev[6], h->st));
+  launch_cmdrift(h->d, h->nblk, h->R, false, h->st);
+  CK(cudaEventRecord(ev[7], h->st));
+  launch_time_advance(h->d, h->R, h->st);
+  CK(cudaEventRecord(ev[8], h->st));
+  CK(cudaEventSynchronize(ev[8]));
+  std::string all;
+  int k = 0;
+  for (; k < 8 && k < max_k; k++) {
+    CK(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
+    all += nm[k];
+    all += "\n";
+  }
+  *n_k = k;
+  std::snprintf(names, names_len, "%s", all.c_str());
+  for (auto& e : ev) cudaEventDestroy(e);
+  h->density_valid = false;
+  if (++h->steps_since_sort >= h->sort_period) {
+    if ((rc = enqueue_reorder(h))) return rc;
+    h->steps_since_sort = 0;
+  }
+  return check_device_error(h);
+}
+
+int idpd_saru_u32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
+                  int32_t draws, uint32_t* out) {
+  idpd_handle* h = nullptr;
+  if (n < 0 || draws < 0 || (n > 0 && (!s1 || !s2 || !s3 || !out)))
+    return fail(nullptr, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0 || draws == 0) return IDPD_OK;
+  uint32_t *d1, *d2, *d3, *dout;
+  CK(cudaMalloc((void**)&d1, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&d2, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&d3, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&dout, 4 * (size_t)n * draws));
+  CK(cudaMemcpy(d1, s1, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d2, s2, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d3, s3, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  launch_saru_test(n, d1, d2, d3, draws, dout, nullptr, 0);
+  CK(cudaMemcpy(out, dout, 4 * (size_t)n * draws, cudaMemcpyDeviceToHost));
+  cudaFree(d1); cudaFree(d2); cudaFree(d3); cudaFree(dout);
+  return IDPD_OK;
+}
+
+int idpd_saru_nrml_f32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
+                       float* out) {
+  idpd_handle* h = nullptr;
+  if (n < 0 || (n > 0 && (!s1 || !s2 || !s3 || !out)))
+    return fail(nullptr, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return IDPD_OK;
+  uint32_t *d1, *d2, *d3;
+  float* dout;
+  CK(cudaMalloc((void**)&d1, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&d2, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&d3, 4 * (size_t)n));
+  CK(cudaMalloc((void**)&dout, 4 * (size_t)n));
+  CK(cudaMemcpy(d1, s1, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d2, s2, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d3, s3, 4 * (size_t)n, cudaMemcpyHostToDevice));
+  launch_saru_test(n, d1, d2, d3, 0, nullptr, dout, 0);
+  CK(cudaMemcpy(out, dout, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+  cudaFree(d1); cudaFree(d2); cudaFree(d3); cudaFree(dout);
+  return IDPD_OK;
+}
+
+int idpd_cell_order(idpd_handle* h, int32_t r, uint32_t* cell_of_row, uint32_t* perm_out) {
+  if (!h || r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  enqueue_cells(h, false);
+  const RepDev& R = h->reps_h[r];
+  const int n = R.n;
+  std::vector<uint32_t> key(n), perm(n), orig(n);
+  CK(cudaMemcpyAsync(key.data(), h->d.key + R.row_off, 4 * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(perm.data(), h->d.perm + R.row_off, 4 * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(orig.data(), h->d.orig + R.row_off, 4 * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int q = 0; q < n; q++) {
+    const uint32_t up = orig[q] - (uint32_t)R.row_off;
+    if (cell_of_row) cell_of_row[up] = key[q] - (uint32_t)R.cell_off;
+    if (perm_out) perm_out[q] = orig[perm[q] - (uint32_t)R.row_off] - (uint32_t)R.row_off;
+  }
+  h->density_valid = false;
+  return check_device_error(h);
+}
+
+}  // extern "C"

@@ -1,0 +1,268 @@
+// Drift and cell binning, the counting sort by cell, and the packed FP32
+// copies that the pair passes read. Replaces the FDPS tree build and the j
+// gather of TreeForForceShort::Gather (src/main.cpp:124-132, 173-174) and
+// performs drift_and_predict (driftkick.hpp:6-27) in the same pass.
+#include "state.cuh"
+
+namespace idpd {
+
+// Periodic wrap of driftkick.hpp:19-21, t - floor(t / L) L with the
+// reference's rounding. Rows that stay inside [0, hi) keep t unchanged
+// without touching the FP64 pipe (the sign bit and the bit pattern order of
+// non-negative doubles decide it); all others take the reference expression.
+__device__ __forceinline__ double wrap_pbc(double t, double L, double iL, long long hi_bits) {
+  const long long b = __double_as_longlong(t);
+  if (b >= 0 && b < hi_bits) return t;
+  const double f = floor(__dmul_rn(t, iL));
+  return __dsub_rn(t, __dmul_rn(f, L));
+}
+
+__device__ __forceinline__ int cell_coord(double x, double inv_cs, int nc) {
+  int c = __double2int_rz(__dmul_rn(x, inv_cs));
+  c = c < 0 ? 0 : c;
+  return c >= nc ? nc - 1 : c;
+}
+
+// One thread per storage row: optional drift, then cell index and arrival slot.
+__global__ void __launch_bounds__(kRowBlock) k_drift_bin(DevState d, int do_drift) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (i >= R->row_off + R->n) return;
+  double x = d.px[i], y = d.py[i], z = d.pz[i];
+  if (do_drift) {
+    const double dt = R->dt;
+    const double h = __dmul_rn(0.5, dt);
+    double p[3] = {x, y, z};
+    double* vv[3] = {d.vx, d.vy, d.vz};
+    double* aa[3] = {d.ax, d.ay, d.az};
+    double* ds[3] = {d.dsx, d.dsy, d.dsz};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double vp = __dadd_rn(vv[k][i], __dmul_rn(h, aa[k][i]));
+      const double dr = __dmul_rn(dt, vp);
+      const double t = __dadd_rn(p[k], dr);
+      ds[k][i] = __dadd_rn(ds[k][i], dr);
+      // hi = L (1 - 2^-50): below it t / L rounds below 1 and floor() is 0.
+      const double L = R->box[k];
+      const long long hi = __double_as_longlong(L) - 4;
+      p[k] = wrap_pbc(t, L, R->ibox[k], hi);
+      vv[k][i] = vp;
+    }
+    x = p[0];
+    y = p[1];
+    z = p[2];
+    d.px[i] = x;
+    d.py[i] = y;
+    d.pz[i] = z;
+  }
+  const int cx = cell_coord(x, R->inv_cs[0], R->nc[0]);
+  const int cy = cell_coord(y, R->inv_cs[1], R->nc[1]);
+  const int cz = cell_coord(z, R->inv_cs[2], R->nc[2]);
+  const uint32_t key = (uint32_t)(R->cell_off + (cz * R->nc[1] + cy) * R->nc[0] + cx);
+  d.key[i] = key;
+  d.slot[i] = (uint32_t)atomicAdd(&d.cell_cnt[key], 1);
+}
+
+// ---------------------------------------------------------------- scan
+constexpr int kScanThreads = 1024;
+constexpr int kScanPerThread = 4;
+constexpr int kScanTile = kScanThreads * kScanPerThread;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int& total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+    int si = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += t;
+    }
+    warp_sums[lane] = si - s;
+    if (lane == 31) warp_sums[32] = si;
+  }
+  __syncthreads();
+  total = warp_sums[32];
+  const int res = incl - v + warp_sums[w];
+  __syncthreads();
+  return res;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* cnt, int* start, int* part,
+                                                             int ncell) {
+  __shared__ int ws[33];
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
+  int c[kScanPerThread];
+  int sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; k++) {
+    c[k] = (base + k < ncell) ? cnt[base + k] : 0;
+    sum += c[k];
+  }
+  int total;
+  int run = block_exclusive_scan(sum, ws, total);
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; k++) {
+    if (base + k < ncell) start[base + k] = run;
+    run += c[k];
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_parts(int* part, int nparts) {
+  __shared__ int ws[33];
+  int carry = 0;
+  for (int b = 0; b < nparts; b += kScanThreads) {
+    const int i = b + threadIdx.x;
+    const int v = i < nparts ? part[i] : 0;
+    int total;
+    const int ex = block_exclusive_scan(v, ws, total);
+    if (i < nparts) part[i] = ex + carry;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_finish(int* cnt, int* start, const int* part,
+                                                              int ncell, int n_tot) {
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
+  const int off = part[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; k++) {
+    if (base + k < ncell) {
+      start[base + k] += off;
+      cnt[base + k] = 0;  // ready for the next binning
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) start[ncell] = n_tot;
+}
+
+void launch_scan(const DevState& d, int ncell_tot, int n_tot, cudaStream_t st) {
+  const int nb = (ncell_tot + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot);
+  k_scan_parts<<<1, kScanThreads, 0, st>>>(d.scan_part, nb);
+  k_scan_finish<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot,
+                                             n_tot);
+}
+
+// ------------------------------------------------- scatter / sort / pack
+__global__ void __launch_bounds__(kRowBlock) k_scatter(DevState d) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (i >= R->row_off + R->n) return;
+  const uint32_t s = (uint32_t)d.cell_start[d.key[i]] + d.slot[i];
+  d.perm[s] = (uint32_t)i;
+}
+
+// Rows of one cell in ascending storage row: the order a stable counting
+// sort gives, independent of the arrival order of the atomics.
+__global__ void k_cell_sort(uint32_t* perm, const int* start, int ncell) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = start[c], e = start[c + 1];
+  for (int k = b + 1; k < e; k++) {
+    const uint32_t v = perm[k];
+    int m = k - 1;
+    while (m >= b && perm[m] > v) {
+      perm[m + 1] = perm[m];
+      m--;
+    }
+    perm[m + 1] = v;
+  }
+}
+
+// One thread per sorted slot: FP32 cell-local position, velocity and ids.
+__global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (s >= R->row_off + R->n) return;
+  const uint32_t i = d.perm[s];
+  d.rank[i] = (uint32_t)s;
+  const uint32_t key = d.key[i];
+  d.scell[s] = key;
+  int cx, cy, cz;
+  cell_xyz((int)key - R->cell_off, R->nc, cx, cy, cz);
+  const float lx = __double2float_rn(__dsub_rn(d.px[i], __dmul_rn((double)cx, R->cs[0])));
+  const float ly = __double2float_rn(__dsub_rn(d.py[i], __dmul_rn((double)cy, R->cs[1])));
+  const float lz = __double2float_rn(__dsub_rn(d.pz[i], __dmul_rn((double)cz, R->cs[2])));
+  d.posf[s] = make_float4(lx, ly, lz, __uint_as_float(d.prop[i]));
+  d.velf[s] = make_float4(__double2float_rn(d.vx[i]), __double2float_rn(d.vy[i]),
+                          __double2float_rn(d.vz[i]), __uint_as_float(d.id[i]));
+}
+
+void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st) {
+  if (nblk == 0) return;
+  k_drift_bin<<<nblk, kRowBlock, 0, st>>>(d, do_drift ? 1 : 0);
+}
+
+void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
+                              cudaStream_t st) {
+  if (nblk == 0) return;
+  k_scatter<<<nblk, kRowBlock, 0, st>>>(d);
+  if (stable) k_cell_sort<<<(ncell_tot + 255) / 256, 256, 0, st>>>(d.perm, d.cell_start, ncell_tot);
+  k_pack<<<nblk, kRowBlock, 0, st>>>(d);
+}
+
+// ------------------------------------------------------------- reorder
+// Moves every storage-order field into sorted order (o holds scratch
+// buffers of the same shape) and rewrites the topology to the new rows.
+__global__ void __launch_bounds__(kRowBlock) k_reorder_gather(DevState d, DevState o) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (s >= R->row_off + R->n) return;
+  const uint32_t i = d.perm[s];
+  o.px[s] = d.px[i]; o.py[s] = d.py[i]; o.pz[s] = d.pz[i];
+  o.vx[s] = d.vx[i]; o.vy[s] = d.vy[i]; o.vz[s] = d.vz[i];
+  o.ax[s] = d.ax[i]; o.ay[s] = d.ay[i]; o.az[s] = d.az[i];
+  o.dsx[s] = d.dsx[i]; o.dsy[s] = d.dsy[i]; o.dsz[s] = d.dsz[i];
+  o.id[s] = d.id[i]; o.prop[s] = d.prop[i]; o.amp_id[s] = d.amp_id[i]; o.unit[s] = d.unit[i];
+  o.orig[s] = d.orig[i];
+  o.key[s] = d.key[i];
+}
+
+__global__ void __launch_bounds__(kRowBlock) k_reorder_loc(DevState d) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (s >= R->row_off + R->n) return;
+  d.loc[d.orig[s]] = (uint32_t)s;
+}
+
+__global__ void k_reorder_topol(uint32_t* topol, const uint32_t* rank, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) topol[k] = rank[topol[k]];
+}
+
+__global__ void __launch_bounds__(kRowBlock) k_identity_perm(DevState d) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (s >= R->row_off + R->n) return;
+  d.perm[s] = (uint32_t)s;
+  d.rank[s] = (uint32_t)s;
+}
+
+void launch_update_loc(const DevState& d, int nblk, cudaStream_t st) {
+  if (nblk == 0) return;
+  k_reorder_loc<<<nblk, kRowBlock, 0, st>>>(d);
+}
+
+void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol, cudaStream_t st) {
+  if (nblk == 0) return;
+  k_reorder_gather<<<nblk, kRowBlock, 0, st>>>(d, o);
+  if (n_topol > 0) k_reorder_topol<<<(n_topol + 255) / 256, 256, 0, st>>>(d.topol, d.rank, n_topol);
+  k_identity_perm<<<nblk, kRowBlock, 0, st>>>(d);
+}
+
+}  // namespace idpd

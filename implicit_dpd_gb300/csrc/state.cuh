@@ -1,0 +1,99 @@
+// Device buffers of one engine handle and the host-side launchers of every
+// kernel. The layout in HBM:
+//   storage order (one row per particle, replicas packed in replica order):
+//     FP64 SoA pos/vel/acc/delta_sumr, u32 id/prop/amp_id/unit, replica, the
+//     upload row (orig) used to hand rows back in upload order;
+//   sorted order (rows grouped by cell, rebuilt every step):
+//     perm (sorted -> storage), rank (storage -> sorted), scell (global cell),
+//     float4 posf (cell-local position, prop bits), velf (velocity, id bits),
+//     densf (partial densities), int64 fixed-point pair force fq[3];
+//   cells: per-cell count and start (exclusive prefix) over all replicas.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace idpd {
+
+struct DevState {
+  // ---- storage order
+  double *px, *py, *pz;
+  double *vx, *vy, *vz;
+  double *ax, *ay, *az;
+  double *dsx, *dsy, *dsz;  // delta_sumr
+  uint32_t *id, *prop, *amp_id, *unit;
+  uint32_t* orig;  // upload row of this storage row
+  uint32_t* loc;   // storage row of each upload row (inverse of orig)
+  // ---- cell build (per step)
+  uint32_t* key;   // global cell of storage row
+  uint32_t* slot;  // arrival slot inside the cell
+  int* cell_cnt;   // [ncell_tot]
+  int* cell_start; // [ncell_tot + 1]
+  int* scan_part;  // block partial sums of the scan
+  // ---- sorted order
+  uint32_t* perm;
+  uint32_t* rank;
+  uint32_t* scell;
+  float4 *posf, *velf, *densf;
+  long long *fqx, *fqy, *fqz;  // pair force, 2^-32 fixed point
+  long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API only)
+  long long *dqx, *dqy, *dqz;  // partial densities, 2^-40 fixed point (fine-grained API only)
+  double* dens64;              // [3N] partial densities of the plain FP64 arm (sorted order)
+  // ---- topology
+  uint32_t* topol;  // [4 * total molecules] storage rows
+  float* cf_bend;   // [total molecules]
+  // ---- replicas and launch maps
+  RepDev* reps;
+  uint32_t* rep_time;  // Parameter::time per replica
+  int* blk_rep;
+  int* blk_row;
+  // ---- reductions
+  double* blk_part;  // [n_blocks * 3]
+  double* rep_mean;  // [R * 3]
+  int* err;          // device error word (0 = ok)
+};
+
+// Error codes written by kernels into DevState::err.
+enum : int { kErrNone = 0, kErrCellOverflow = 1, kErrBadCell = 2, kErrListOverflow = 3,
+             kErrNonFinite = 4, kErrComBox = 5 };
+
+constexpr int kRowBlock = 128;  // rows per block of row-block launches
+
+// kernels_cells.cu
+void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st);
+void launch_scan(const DevState& d, int ncell_tot, int n_tot, cudaStream_t st);
+void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
+                              cudaStream_t st);
+void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol,
+                    cudaStream_t st);
+void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
+
+// kernels_pairs.cu
+struct PairTuning {
+  int list_cap;    // neighbour slots per thread in shared memory
+  int block;       // threads per block (multiple of 32, <= kRowBlock)
+};
+void launch_density(const DevState& d, int nblk, bool fp64, cudaStream_t st);
+void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
+                  cudaStream_t st);
+void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
+
+// kernels_integrate.cu
+void launch_bonded_kick(const DevState& d, int nblk, bool kick, cudaStream_t st);
+void launch_bonded_fine(const DevState& d, int n_amp_tot, const int* amp_rep, double* vir_part,
+                        cudaStream_t st);
+void launch_kick_only(const DevState& d, int nblk, cudaStream_t st);
+void launch_fq_to_acc(const DevState& d, int nblk, double* press_out, cudaStream_t st);
+void launch_cmdrift(const DevState& d, int nblk, int R, bool force_now, cudaStream_t st);
+void launch_time_advance(const DevState& d, int R, cudaStream_t st);
+void launch_saru_test(int n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3, int draws,
+                      uint32_t* out_u, float* out_n, cudaStream_t st);
+void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n, cudaStream_t st);
+void launch_set_dynamics(const DevState& d, const double* aos3x3, int row0, int n, double box0,
+                         double box1, double box2, cudaStream_t st);
+void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* orig,
+                       int row0, double* aos, int n, cudaStream_t st);
+
+}  // namespace idpd

@@ -1,0 +1,245 @@
+"""ctypes binding of the engine's C ABI (include/idpd_engine.h).
+
+This is plumbing for tests and the benchmark; C and C++ callers link the
+library directly (include/idpd/reference_api.hpp). The library is built
+in-tree by implicit_dpd_gb300/build.py; loading fails loudly when it is
+missing, there is no fallback path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import STATUS_NAMES, IdpdConfig, IdpdParams, IdpdRunParam
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
+
+D = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+U = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+F = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+VP = C.c_void_p
+
+# every symbol include/idpd_engine.h declares (tests/test_abi.py checks them)
+EXPORTS = [
+    "idpd_derive_params", "idpd_create", "idpd_destroy", "idpd_last_error", "idpd_set_params",
+    "idpd_get_params", "idpd_upload_state", "idpd_num_particles", "idpd_download_state",
+    "idpd_download_aux", "idpd_build_topology", "idpd_drift", "idpd_density", "idpd_force",
+    "idpd_bonded", "idpd_kick", "idpd_remove_cmdrift", "idpd_step", "idpd_sync",
+    "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
+    "idpd_cell_order", "idpd_set_dynamics",
+]
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise EngineError(f"engine library not built: {path} (run implicit_dpd_gb300.build)")
+    L = C.CDLL(path)
+    H = C.c_void_p
+    L.idpd_derive_params.argtypes = [C.POINTER(IdpdRunParam), C.POINTER(IdpdParams)]
+    L.idpd_create.argtypes = [C.POINTER(IdpdConfig), C.POINTER(H)]
+    L.idpd_destroy.argtypes = [H]
+    L.idpd_last_error.argtypes = [H, C.c_char_p, C.c_size_t]
+    L.idpd_set_params.argtypes = [H, C.c_int32, C.POINTER(IdpdParams)]
+    L.idpd_get_params.argtypes = [H, C.c_int32, C.POINTER(IdpdParams)]
+    L.idpd_upload_state.argtypes = [H, C.c_int32, C.c_int32, D, D, VP, U, U, VP, VP]
+    L.idpd_num_particles.argtypes = [H, C.c_int32, C.POINTER(C.c_int32)]
+    L.idpd_download_state.argtypes = [H, C.c_int32, VP, VP, VP, VP, VP, VP, VP]
+    L.idpd_download_aux.argtypes = [H, C.c_int32, VP, VP, VP, VP]
+    L.idpd_build_topology.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, VP]
+    for name in ("idpd_drift", "idpd_density", "idpd_force", "idpd_kick", "idpd_remove_cmdrift",
+                 "idpd_sync"):
+        getattr(L, name).argtypes = [H]
+    L.idpd_bonded.argtypes = [H, VP]
+    L.idpd_step.argtypes = [H, C.c_int32]
+    L.idpd_last_step_ms.argtypes = [H, C.POINTER(C.c_float)]
+    L.idpd_profile_step.argtypes = [H, C.c_char_p, C.c_size_t, F, C.c_int32, C.POINTER(C.c_int32)]
+    L.idpd_saru_u32.argtypes = [C.c_int32, U, U, U, C.c_int32, U]
+    L.idpd_saru_nrml_f32.argtypes = [C.c_int32, U, U, U, F]
+    L.idpd_cell_order.argtypes = [H, C.c_int32, VP, VP]
+    L.idpd_set_dynamics.argtypes = [H, C.c_int32, VP, VP, VP]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def last_error(h=None):
+    buf = C.create_string_buffer(512)
+    load().idpd_last_error(h, buf, 512)
+    return buf.value.decode()
+
+
+def check(rc, h=None, what=""):
+    if rc != 0:
+        raise EngineError(f"{what}: {STATUS_NAMES.get(rc, rc)}: {last_error(h)}")
+
+
+def derive_params(rp):
+    out = IdpdParams()
+    check(load().idpd_derive_params(C.byref(rp), C.byref(out)), None, "derive_params")
+    return out
+
+
+def saru_u32(s1, s2, s3, draws):
+    s1, s2, s3 = (np.ascontiguousarray(x, np.uint32) for x in (s1, s2, s3))
+    out = np.zeros(len(s1) * draws, np.uint32)
+    check(load().idpd_saru_u32(len(s1), s1, s2, s3, draws, out), None, "saru_u32")
+    return out.reshape(len(s1), draws)
+
+
+def saru_nrml_f32(s1, s2, s3):
+    s1, s2, s3 = (np.ascontiguousarray(x, np.uint32) for x in (s1, s2, s3))
+    out = np.zeros(len(s1), np.float32)
+    check(load().idpd_saru_nrml_f32(len(s1), s1, s2, s3, out), None, "saru_nrml_f32")
+    return out
+
+
+class Engine:
+    """One engine handle (idpd_handle*)."""
+
+    def __init__(self, n_replicas=1, device=0, flags=0, sort_period=0, capacity=0):
+        L = load()
+        cfg = IdpdConfig(n_replicas=n_replicas, capacity=capacity, device=device, flags=flags,
+                         sort_period=sort_period)
+        h = C.c_void_p()
+        check(L.idpd_create(C.byref(cfg), C.byref(h)), None, "idpd_create")
+        self.h = h
+        self.L = L
+        self.R = n_replicas
+
+    def close(self):
+        if self.h:
+            self.L.idpd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        check(rc, self.h, what)
+
+    def set_params(self, p, replica=0):
+        self._ck(self.L.idpd_set_params(self.h, replica, C.byref(p)), "set_params")
+
+    def get_params(self, replica=0):
+        p = IdpdParams()
+        self._ck(self.L.idpd_get_params(self.h, replica, C.byref(p)), "get_params")
+        return p
+
+    def upload(self, st, replica=0):
+        n = len(st["pos"])
+        acc = st.get("acc")
+        self._ck(self.L.idpd_upload_state(
+            self.h, replica, n, np.ascontiguousarray(st["pos"], np.float64),
+            np.ascontiguousarray(st["vel"], np.float64),
+            _p(None if acc is None else np.ascontiguousarray(acc, np.float64)),
+            np.ascontiguousarray(st["id"], np.uint32), np.ascontiguousarray(st["prop"], np.uint32),
+            _p(np.ascontiguousarray(st["amp_id"], np.uint32)) if "amp_id" in st else None,
+            _p(np.ascontiguousarray(st["unit"], np.uint32)) if "unit" in st else None), "upload")
+
+    def set_dynamics(self, pos, vel, acc, replica=0):
+        """pos/vel/acc: C-contiguous float64 (n, 3) arrays (pinned for speed)."""
+        self._ck(self.L.idpd_set_dynamics(self.h, replica, _p(pos), _p(vel), _p(acc)),
+                 "set_dynamics")
+
+    def download_dynamics(self, pos, vel, acc, replica=0):
+        """Fills caller-provided (n, 3) float64 arrays, e.g. pinned buffers."""
+        self._ck(self.L.idpd_download_state(self.h, replica, _p(pos), _p(vel), _p(acc), None, None,
+                                            None, None), "download_dynamics")
+
+    def num_particles(self, replica=0):
+        n = C.c_int32()
+        self._ck(self.L.idpd_num_particles(self.h, replica, C.byref(n)), "num_particles")
+        return n.value
+
+    def build_topology(self, n_amp, core_amp_id=(), replica=0):
+        core = np.ascontiguousarray(list(core_amp_id) or [0], np.uint32)
+        self._ck(self.L.idpd_build_topology(self.h, replica, n_amp, len(core_amp_id), _p(core)),
+                 "build_topology")
+
+    def download(self, replica=0):
+        n = self.num_particles(replica)
+        out = {k: np.zeros((n, 3)) for k in ("pos", "vel", "acc")}
+        for k in ("id", "prop", "amp_id", "unit"):
+            out[k] = np.zeros(n, np.uint32)
+        self._ck(self.L.idpd_download_state(self.h, replica, _p(out["pos"]), _p(out["vel"]),
+                                            _p(out["acc"]), _p(out["id"]), _p(out["prop"]),
+                                            _p(out["amp_id"]), _p(out["unit"])), "download")
+        return out
+
+    def download_aux(self, replica=0, density=True, press=False, nei_cm=False, dsr=False):
+        n = self.num_particles(replica)
+        out = {}
+        if density:
+            out["dens"] = np.zeros((n, 3))
+        if press:
+            out["press"] = np.zeros((n, 3))
+        if nei_cm:
+            out["nei_cm"] = np.zeros((n, 6))
+        if dsr:
+            out["dsr"] = np.zeros((n, 3))
+        self._ck(self.L.idpd_download_aux(self.h, replica, _p(out.get("dens")),
+                                          _p(out.get("press")), _p(out.get("nei_cm")),
+                                          _p(out.get("dsr"))), "download_aux")
+        return out
+
+    def drift(self):
+        self._ck(self.L.idpd_drift(self.h), "drift")
+
+    def density(self):
+        self._ck(self.L.idpd_density(self.h), "density")
+
+    def force(self):
+        self._ck(self.L.idpd_force(self.h), "force")
+
+    def bonded(self):
+        vir = np.zeros(3 * self.R)
+        self._ck(self.L.idpd_bonded(self.h, _p(vir)), "bonded")
+        return vir.reshape(self.R, 3)
+
+    def kick(self):
+        self._ck(self.L.idpd_kick(self.h), "kick")
+
+    def remove_cmdrift(self):
+        self._ck(self.L.idpd_remove_cmdrift(self.h), "remove_cmdrift")
+
+    def step(self, nsteps=1):
+        self._ck(self.L.idpd_step(self.h, nsteps), "step")
+
+    def sync(self):
+        self._ck(self.L.idpd_sync(self.h), "sync")
+
+    def last_step_ms(self):
+        v = C.c_float()
+        self._ck(self.L.idpd_last_step_ms(self.h, C.byref(v)), "last_step_ms")
+        return v.value
+
+    def profile_step(self):
+        names = C.create_string_buffer(1024)
+        ms = np.zeros(32, np.float32)
+        nk = C.c_int32()
+        self._ck(self.L.idpd_profile_step(self.h, names, 1024, ms, 32, C.byref(nk)), "profile_step")
+        keys = names.value.decode().split()
+        return dict(zip(keys, ms[: nk.value].tolist()))
+
+    def cell_order(self, replica=0):
+        n = self.num_particles(replica)
+        cell = np.zeros(n, np.uint32)
+        perm = np.zeros(n, np.uint32)
+        self._ck(self.L.idpd_cell_order(self.h, replica, _p(cell), _p(perm)), "cell_order")
+        return cell, perm

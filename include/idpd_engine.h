@@ -126,6 +126,13 @@ int idpd_upload_state(idpd_handle* h, int32_t replica, int32_t n, const double* 
                       const double* vel, const double* acc, const uint32_t* id,
                       const uint32_t* prop, const uint32_t* amp_id, const uint32_t* unit);
 int idpd_num_particles(const idpd_handle* h, int32_t replica, int32_t* n);
+/* Per-step exchange for a host that keeps the particle state (the FDPS
+ * driver loop, src/main.cpp:166-184): overwrites pos/vel/acc of the rows of
+ * an uploaded replica, in upload order, keeping ids, properties and the
+ * topology. Positions outside [0, box] or non-finite values are rejected by
+ * the device and reported by the next call. */
+int idpd_set_dynamics(idpd_handle* h, int32_t replica, const double* pos, const double* vel,
+                      const double* acc);
 /* Any pointer may be NULL to skip that field. Rows come back in the order
  * they were uploaded (new particles from chemistry appended). */
 int idpd_download_state(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc,
