@@ -86,6 +86,10 @@ class IdpdConfig(C.Structure):
     ]
 
 
+class IdpdTuning(C.Structure):
+    _fields_ = [("reach", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
 def params_to_dict(p):
     import numpy as np
 

@@ -101,3 +101,34 @@ def run_param(box, dt=0.005, cf_r=3.0, cf_s=50.0, cf_b=10.0, cf_b_rigid=None, vb
     rp.kappa = f32(kappa)
     rp.rho_co = f32(rho_co)
     return rp
+
+
+def tile(st, box, reps):
+    """Periodic copies of a system: reps = (nx, ny, nz) copies along each axis.
+
+    Copy c of row i gets id = c * n + i and, for molecule rows,
+    amp_id = c * n_amp + amp_id (n_amp = 1 + the largest amp_id); solvent rows
+    keep amp_id = unit = 0xffffffff. Returns (state, box * reps)."""
+    box = np.asarray(box, np.float64)
+    reps = np.asarray(reps, int)
+    n = len(st["pos"])
+    mol = st["amp_id"] != NONE32
+    n_amp = int(st["amp_id"][mol].max()) + 1 if mol.any() else 0
+    out = {k: [] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")}
+    c = 0
+    for iz in range(reps[2]):
+        for iy in range(reps[1]):
+            for ix in range(reps[0]):
+                shift = np.array([ix, iy, iz]) * box
+                out["pos"].append(st["pos"] + shift)
+                out["vel"].append(st["vel"])
+                out["acc"].append(st["acc"])
+                out["id"].append((st["id"].astype(np.int64) + c * n).astype(np.uint32))
+                out["prop"].append(st["prop"])
+                a = st["amp_id"].astype(np.int64)
+                out["amp_id"].append(np.where(mol, a + c * n_amp, NONE32).astype(np.uint32))
+                out["unit"].append(st["unit"])
+                c += 1
+    res = {k: np.concatenate(v) for k, v in out.items()}
+    res["pos"] = np.ascontiguousarray(res["pos"])
+    return res, box * reps

@@ -28,6 +28,10 @@ constexpr float kDensScaleF = 1099511627776.0f;
 constexpr double kDensUnscale = 1.0 / 1099511627776.0;
 constexpr double kPosScale = 1099511627776.0;         // 2^40: COM sums, delta_sumr
 constexpr float kPosScaleF = 1099511627776.0f;
+constexpr int kForceBits = 32;
+constexpr int kDensBits = 40;
+constexpr int kPosBits = 40;
+constexpr float kDensUnscaleF = 1.0f / 1099511627776.0f;
 
 // FP32 pair-set decisions within this band of a cutoff are re-taken in FP64
 // from the FP64 positions, exactly as the reference's FP64 test. The bound on
@@ -41,7 +45,8 @@ struct RepDev {
   double ibox[3];    // 1 / box (Parameter::ibox_leng)
   double inv_cs[3];  // cells per unit length (nc / box)
   double cs[3];      // cell side (box / nc)
-  float cs_f[3];
+  float cs_f[3];     // cell side rounded to float
+  float cs_lo[3];    // cs - cs_f
   int nc[3];
   int cell_off;      // first global cell of the replica
   int ncell;
@@ -57,6 +62,13 @@ struct RepDev {
   int form;
   int n_amp;         // molecules of the replica
   int amp_off;       // first molecule slot in the global topology
+  int reach;         // cells per cutoff: cell side >= 1 / reach, stencil (2 reach + 1)^3
+};
+
+// FP64 coefficient tables of a replica (plain FP64 kernels).
+struct RepTab64 {
+  double cf_c[9], cf_g[9], cf_r[9], cf_m[27];
+  double wa, wb, wrd;
 };
 
 // Row-block launch: block b covers rows [blk_row[b], blk_row[b] + blockDim)
@@ -123,6 +135,76 @@ __device__ __forceinline__ double saru_nrml_f64(Saru& s) {
   const double u1 = ((double)(int)(s.next() >> 1) + 0.5) * (1.0 / 2147483648.0);
   const double u2 = ((double)(int)(s.next() >> 1) + 0.5) * (1.0 / 2147483648.0);
   return sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
+}
+
+// Splits a double X (|X| < 2^8) into floats hi + lo with |X - hi - lo| below
+// 2^-47 |X|, with integer operations only: hi keeps the leading 24 mantissa
+// bits (truncated), lo the remaining 29 bits rounded to float.
+__device__ __forceinline__ void split_double(double X, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(X);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)(b >> 52) & 0x7ff;
+  if (e < 897) {  // |X| < 2^-126: both parts are negligible
+    hi = 0.0f;
+    lo = 0.0f;
+    return;
+  }
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const uint32_t hm = (uint32_t)(m >> 29);
+  hi = __uint_as_float(sign | ((uint32_t)(e - 896) << 23) | (hm & 0x7FFFFFu));
+  if (e < 949) {
+    lo = 0.0f;
+  } else {
+    const float scale = __uint_as_float((uint32_t)(e - 948) << 23);  // 2^(e - 1075)
+    lo = __uint_as_float(__float_as_uint(__uint2float_rn((uint32_t)(m & 0x1FFFFFFFull)) * scale) |
+                         sign);
+  }
+}
+
+// Error-free transforms (Knuth's TwoSum, fma-based TwoProduct).
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+  const float s = a + b;
+  const float bb = s - a;
+  err = (a - (s - bb)) + (b - bb);
+  return s;
+}
+__device__ __forceinline__ float two_prod(float a, float b, float& err) {
+  const float p = a * b;
+  err = fmaf(a, b, -p);
+  return p;
+}
+
+// Round(v * 2^S) as int64 from the float's bits, without conversion
+// instructions (float-to-int64 conversion runs on the FP64 pipe).
+// Ties round away from zero; |v| 2^S must stay below 2^62.
+__device__ __forceinline__ long long fix_from_float(float v, int S) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 150 + S;
+  long long q;
+  if (sh >= 0)
+    q = m << (sh < 39 ? sh : 39);
+  else
+    q = sh > -25 ? (m + (1ll << (-sh - 1))) >> (-sh) : 0ll;
+  q = e == 0 ? 0ll : q;
+  return (b >> 31) ? -q : q;
+}
+
+// Fixed-point sum back to float: two exact 32-bit halves.
+__device__ __forceinline__ float fix_to_float(long long q, float unscale) {
+  const float hi = (float)(int)(q >> 32) * 4294967296.0f;
+  const float lo = (float)(uint32_t)(q & 0xffffffffll);
+  return (hi + lo) * unscale;
+}
+
+// Fixed-point sum to double, exactly for |q| < 2^51: the integer is added
+// into the mantissa of 1.5 * 2^52 and the bias removed with one FP64 add
+// (an int64-to-double conversion is a slower FP64-pipe instruction).
+__device__ __forceinline__ double fix_to_double(long long q, double unscale) {
+  const double magic = 6755399441055744.0;  // 1.5 * 2^52
+  const double v = __longlong_as_double(q + __double_as_longlong(magic)) - magic;
+  return v * unscale;
 }
 
 // Float with bits reinterpreted as a uint32 payload (prop / id in .w lanes).

@@ -62,7 +62,7 @@ struct idpd_handle {
   cudaGraphExec_t graph = nullptr;
   int steps_since_sort = 0;
   float last_ms = 0.f;
-  PairTuning tune{48, kRowBlock};
+  PairTuning tune{1};
   std::string err;
 };
 
@@ -140,14 +140,16 @@ int check_params(idpd_handle* h, const idpd_params* p) {
   return IDPD_OK;
 }
 
-void fill_repdev(RepDev& R, const idpd_params& p) {
+void fill_repdev(RepDev& R, const idpd_params& p, int reach) {
+  R.reach = reach;
   for (int k = 0; k < 3; k++) {
     R.box[k] = p.box[k];
     R.ibox[k] = 1.0 / p.box[k];
-    R.nc[k] = (int)(p.box[k] / 1.0);
+    R.nc[k] = (int)(p.box[k] * (double)reach);
     R.inv_cs[k] = (double)R.nc[k] / p.box[k];
     R.cs[k] = p.box[k] / (double)R.nc[k];
     R.cs_f[k] = (float)R.cs[k];
+    R.cs_lo[k] = (float)(R.cs[k] - (double)R.cs_f[k]);
   }
   R.ncell = R.nc[0] * R.nc[1] * R.nc[2];
   R.dt = p.dt;
@@ -199,11 +201,12 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.cell_start, cc + 1);
   AL(d.scan_part, (cc + 4095) / 4096 + 1);
   AL(d.perm, cap); AL(d.rank, cap); AL(d.scell, cap);
-  AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap);
+  AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap); AL(d.poslo, cap);
   AL(d.fqx, cap); AL(d.fqy, cap); AL(d.fqz, cap);
   AL(d.topol, 4 * ac);
   AL(d.cf_bend, ac);
   AL(d.reps, h->R);
+  AL(d.tab64, h->R);
   AL(d.rep_time, h->R);
   AL(d.blk_rep, bc);
   AL(d.blk_row, bc);
@@ -256,7 +259,7 @@ int commit(idpd_handle* h) {
     std::vector<int> blk_rep, blk_row;
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
-      fill_repdev(R, h->params[r]);
+      fill_repdev(R, h->params[r], h->tune.reach);
       R.row_off = row;
       R.n = h->n[r];
       R.cell_off = cell;
@@ -346,15 +349,71 @@ int commit(idpd_handle* h) {
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
       const RepDev keep = R;
-      fill_repdev(R, h->params[r]);
+      fill_repdev(R, h->params[r], h->tune.reach);
       R.row_off = keep.row_off; R.n = keep.n; R.cell_off = keep.cell_off; R.blk_off = keep.blk_off;
       R.nblk = keep.nblk; R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
       if (R.ncell != keep.ncell) return fail(h, IDPD_ERR_STATE, "box change alters the cell grid; re-upload the state");
     }
     CK(cudaMemcpyAsync(h->d.reps, h->reps_h.data(), sizeof(RepDev) * h->R, cudaMemcpyHostToDevice, h->st));
+    std::vector<RepTab64> t64(h->R);
+    for (int r = 0; r < h->R; r++) {
+      const idpd_params& p = h->params[r];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          t64[r].cf_c[3 * i + j] = p.cf_c[i][j];
+          t64[r].cf_g[3 * i + j] = p.cf_g[i][j];
+          t64[r].cf_r[3 * i + j] = p.cf_r[i][j];
+          for (int k = 0; k < 3; k++) t64[r].cf_m[9 * i + 3 * j + k] = p.cf_m[i][j][k];
+        }
+      t64[r].wa = p.warren_a;
+      t64[r].wb = p.warren_b;
+      t64[r].wrd = p.form == IDPD_FORM_WARREN ? p.warren_rd : 1.0;
+    }
+    CK(cudaMemcpyAsync(h->d.tab64, t64.data(), sizeof(RepTab64) * h->R, cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
     h->reps_dirty = false;
   }
+  return IDPD_OK;
+}
+
+// (Re)allocates only the cell arrays, keeping the particle arrays.
+int realloc_cells(idpd_handle* h, int ncell) {
+  DevState& d = h->d;
+  if (ncell > h->ncell_cap) {
+    for (void* p : {(void*)d.cell_cnt, (void*)d.cell_start, (void*)d.scan_part}) {
+      h->allocs.erase(std::remove(h->allocs.begin(), h->allocs.end(), p), h->allocs.end());
+      cudaFree(p);
+    }
+    int rc;
+    if ((rc = dalloc(h, &d.cell_cnt, ncell)) || (rc = dalloc(h, &d.cell_start, ncell + 1)) ||
+        (rc = dalloc(h, &d.scan_part, (ncell + 4095) / 4096 + 1)))
+      return rc;
+    h->ncell_cap = ncell;
+  }
+  CK(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * h->ncell_cap, h->st));
+  return IDPD_OK;
+}
+
+// Applies a new cell reach to a committed layout: new cell grids and cell
+// offsets, same particle rows.
+int retune_cells(idpd_handle* h) {
+  invalidate_graph(h);
+  int cell = 0;
+  for (int r = 0; r < h->R; r++) {
+    RepDev& R = h->reps_h[r];
+    const RepDev keep = R;
+    fill_repdev(R, h->params[r], h->tune.reach);
+    R.row_off = keep.row_off; R.n = keep.n; R.blk_off = keep.blk_off; R.nblk = keep.nblk;
+    R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
+    R.cell_off = cell;
+    cell += R.ncell;
+  }
+  h->ncell_tot = cell;
+  int rc = realloc_cells(h, cell);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->d.reps, h->reps_h.data(), sizeof(RepDev) * h->R, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->density_valid = false;
   return IDPD_OK;
 }
 
@@ -913,6 +972,23 @@ int idpd_sync(idpd_handle* h) {
   cudaSetDevice(h->device);
   CK(cudaStreamSynchronize(h->st));
   return check_device_error(h);
+}
+
+int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
+  if (!h || !t) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
+  if (t->reach < 1 || t->reach > 2) return fail(h, IDPD_ERR_INVALID_ARG, "reach must be 1 or 2");
+  cudaSetDevice(h->device);
+  const bool changed = t->reach != h->tune.reach;
+  h->tune.reach = t->reach;
+  if (changed && h->on_device && !h->layout_dirty) return retune_cells(h);
+  return IDPD_OK;
+}
+
+int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t) {
+  if (!h || !t) return IDPD_ERR_INVALID_ARG;
+  std::memset(t, 0, sizeof(*t));
+  t->reach = h->tune.reach;
+  return IDPD_OK;
 }
 
 int idpd_last_step_ms(const idpd_handle* h, float* ms) {

@@ -192,10 +192,14 @@ __global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
   d.scell[s] = key;
   int cx, cy, cz;
   cell_xyz((int)key - R->cell_off, R->nc, cx, cy, cz);
-  const float lx = __double2float_rn(__dsub_rn(d.px[i], __dmul_rn((double)cx, R->cs[0])));
-  const float ly = __double2float_rn(__dsub_rn(d.py[i], __dmul_rn((double)cy, R->cs[1])));
-  const float lz = __double2float_rn(__dsub_rn(d.pz[i], __dmul_rn((double)cz, R->cs[2])));
+  // x - cx cs is exact in FP64 (Sterbenz: x lies in [o, 2o] or o = 0); its
+  // float split keeps 48 bits for the near-cutoff pair terms.
+  float lx, ly, lz, ex, ey, ez;
+  split_double(__dsub_rn(d.px[i], __dmul_rn((double)cx, R->cs[0])), lx, ex);
+  split_double(__dsub_rn(d.py[i], __dmul_rn((double)cy, R->cs[1])), ly, ey);
+  split_double(__dsub_rn(d.pz[i], __dmul_rn((double)cz, R->cs[2])), lz, ez);
   d.posf[s] = make_float4(lx, ly, lz, __uint_as_float(d.prop[i]));
+  d.poslo[s] = make_float4(ex, ey, ez, 0.0f);
   d.velf[s] = make_float4(__double2float_rn(d.vx[i]), __double2float_rn(d.vy[i]),
                           __double2float_rn(d.vz[i]), __uint_as_float(d.id[i]));
 }

@@ -103,12 +103,12 @@ __global__ void __launch_bounds__(kRowBlock) k_bonded_kick(DevState d) {
 #pragma unroll
     for (int k = 1; k < 4; k++)
       if (k == u) fu = F[k];
-    f[0] += __float2ll_rn(fu.x * kForceScaleF);
-    f[1] += __float2ll_rn(fu.y * kForceScaleF);
-    f[2] += __float2ll_rn(fu.z * kForceScaleF);
+    f[0] += fix_from_float(fu.x, kForceBits);
+    f[1] += fix_from_float(fu.y, kForceBits);
+    f[2] += fix_from_float(fu.z, kForceBits);
   }
-  const double acx = (double)f[0] * kForceUnscale, acy = (double)f[1] * kForceUnscale,
-               acz = (double)f[2] * kForceUnscale;
+  const double acx = fix_to_double(f[0], kForceUnscale), acy = fix_to_double(f[1], kForceUnscale),
+               acz = fix_to_double(f[2], kForceUnscale);
   d.ax[i] = acx;
   d.ay[i] = acy;
   d.az[i] = acz;

@@ -1,43 +1,28 @@
 // The two MDPD passes over the cell list:
 //   pass 1, CalcDensity::operator() (nbdf_calculator.hpp:11-60);
 //   pass 2, CalcForceEpEpDPD::operator() (nbdf_calculator.hpp:63-145).
-// The FP32 kernels form each pair vector from cell-local FP32 coordinates
-// (error below 5e-7 per component, independent of the box size), take every
-// cutoff decision within kGuard of the cutoff again in FP64 from the FP64
-// positions exactly as the reference does (so pair sets are the reference's),
-// and sum every pair term as a 64-bit fixed-point integer, which makes the
-// result independent of the visiting order and of the launch shape.
-// The plain FP64 kernels are the single-system FP64 baseline: the same cell
-// list, FP64 throughout, FP64 sums in cell order.
+//
+// FP32 passes (the engine): one warp per particle. The warp caches the
+// neighbour-cell segments of the particle's cell in shared memory, sweeps
+// each segment 32 candidates at a time (coalesced float4 loads), and for
+// pass 2 appends the in-range pairs to a warp queue that is evaluated 32
+// pairs at a time with every lane busy. Pair vectors come from cell-local
+// FP32 coordinates; cutoff decisions within kGuard of the cutoff are re-taken
+// in FP64 from the FP64 positions as the reference takes them; pairs within
+// 0.01 of the cutoff take 1 - r from the compensated (hi + lo) coordinates;
+// every pair term is summed as a 64-bit fixed-point integer, so the result is
+// independent of the visiting order, of the cell size and of the launch shape.
+//
+// FP64 passes (the plain single-system baseline): one thread per particle,
+// FP64 throughout, FP64 sums in cell order.
 #include "state.cuh"
 
 namespace idpd {
 
-// Pair vector test of one neighbour cell: visits every (dx, dy, dz) in
-// dz-major order with the wrapped cell, its FP32 offset and its image shift.
-template <class F>
-__device__ __forceinline__ void for_each_cell27(const RepDev* R, int cx, int cy, int cz, F&& f) {
-  const int nx = R->nc[0], ny = R->nc[1], nz = R->nc[2];
-#pragma unroll 1
-  for (int dz = -1; dz <= 1; dz++) {
-    const int qz = cz + dz;
-    const int sz = qz < 0 ? -1 : (qz >= nz ? 1 : 0);
-    const int wz = qz - sz * nz;
-#pragma unroll 1
-    for (int dy = -1; dy <= 1; dy++) {
-      const int qy = cy + dy;
-      const int sy = qy < 0 ? -1 : (qy >= ny ? 1 : 0);
-      const int wy = qy - sy * ny;
-      const int row = R->cell_off + (wz * ny + wy) * nx;
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
-      for (int dx = -1; dx <= 1; dx++) {
-        const int qx = cx + dx;
-        const int sx = qx < 0 ? -1 : (qx >= nx ? 1 : 0);
-        const int wx = qx - sx * nx;
-        f(row + wx, dx, dy, dz, sx, sy, sz);
-      }
-    }
-  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // FP64 squared distance of rows i and j (image shift s * L applied to j),
@@ -52,59 +37,181 @@ __device__ __forceinline__ double exact_dr2(const DevState& d, const RepDev* R, 
   return __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
 }
 
-__device__ __forceinline__ long long to_fix(float v, float scale) {
-  return __float2ll_rn(v * scale);
+// ------------------------------------------------ neighbour segments
+// A segment is a run of x-consecutive cells of one (dy, dz) row with one
+// image shift; its rows are contiguous in sorted order. Interior cell
+// boundaries give each candidate its x-cell offset.
+constexpr int kMaxReach = 2;
+constexpr int kMaxSeg = 2 * (2 * kMaxReach + 1) * (2 * kMaxReach + 1);  // 50
+constexpr int kWarps = kRowBlock / 32;
+
+struct SegTable {
+  int tb[kMaxSeg], te[kMaxSeg];
+  int bnd[kMaxSeg][2 * kMaxReach];  // start of the 2nd.. cells (INT_MAX when absent)
+  int code[kMaxSeg];                // dx0+4 | (dy+4)<<3 | (dz+4)<<6 | (sx+1)<<9 | (sy+1)<<11 | (sz+1)<<13
+};
+
+// Lane k < (2m+1)^2 builds the (up to two) segments of row k of cell
+// (cx, cy, cz); slots of a row that do not exist are left empty.
+__device__ __forceinline__ void build_segments(SegTable& S, const DevState& d, const RepDev* R,
+                                               int cx, int cy, int cz, int lane) {
+  const int m = R->reach, w = 2 * m + 1;
+  const int nx = R->nc[0], ny = R->nc[1], nz = R->nc[2];
+  for (int k = lane; k < w * w; k += 32) {
+    const int dz = k / w - m, dy = k % w - m;
+    const int qz = cz + dz, sz = qz < 0 ? -1 : (qz >= nz ? 1 : 0), wz = qz - sz * nz;
+    const int qy = cy + dy, sy = qy < 0 ? -1 : (qy >= ny ? 1 : 0), wy = qy - sy * ny;
+    const int base = R->cell_off + (wz * ny + wy) * nx;
+    // parts: [cx-m, -1] wrapped left (sx=-1), [max(cx-m,0), min(cx+m,nx-1)] (sx=0),
+    // [nx, cx+m] wrapped right (sx=+1); at most two are non-empty.
+    int slot = 2 * k;
+    for (int part = -1; part <= 1; part++) {
+      int lo, hi;  // unwrapped offsets lo..hi; wrapped index = cx + off - part * nx
+      if (part == -1) {
+        lo = -m;
+        hi = -cx - 1;
+      } else if (part == 0) {
+        lo = cx - m < 0 ? -cx : -m;
+        hi = cx + m >= nx ? nx - 1 - cx : m;
+      } else {
+        lo = nx - cx;
+        hi = m;
+      }
+      if (lo > hi) continue;
+      const int xs = cx + lo - part * nx;
+      const int ncells = hi - lo + 1;
+      S.tb[slot] = d.cell_start[base + xs];
+      S.te[slot] = d.cell_start[base + xs + ncells];
+#pragma unroll
+      for (int q = 0; q < 2 * kMaxReach; q++)
+        S.bnd[slot][q] = q + 1 < ncells ? d.cell_start[base + xs + q + 1] : 0x7fffffff;
+      S.code[slot] = (lo + 4) | ((dy + 4) << 3) | ((dz + 4) << 6) | ((part + 1) << 9) |
+                     ((sy + 1) << 11) | ((sz + 1) << 13);
+      slot++;
+    }
+    for (; slot < 2 * k + 2; slot++) {
+      S.tb[slot] = 0;
+      S.te[slot] = 0;
+    }
+  }
+}
+
+__device__ __forceinline__ int seg_dx(const SegTable& S, int g, int t) {
+  int dx = (S.code[g] & 7) - 4;
+#pragma unroll
+  for (int q = 0; q < 2 * kMaxReach; q++) dx += t >= S.bnd[g][q];
+  return dx;
+}
+
+struct PairCode {
+  int dx, dy, dz, sx, sy, sz;
+};
+__device__ __forceinline__ uint32_t pack_code(int dx, int seg_code) {
+  return (uint32_t)((dx + 4) | (seg_code & ~7));
+}
+__device__ __forceinline__ PairCode unpack_code(uint32_t c) {
+  PairCode p;
+  p.dx = (int)(c & 7) - 4;
+  p.dy = (int)((c >> 3) & 7) - 4;
+  p.dz = (int)((c >> 6) & 7) - 4;
+  p.sx = (int)((c >> 9) & 3) - 1;
+  p.sy = (int)((c >> 11) & 3) - 1;
+  p.sz = (int)((c >> 13) & 3) - 1;
+  return p;
 }
 
 // ------------------------------------------------------------- pass 1
 __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
+  __shared__ SegTable seg[kWarps];
   const int r = d.blk_rep[blockIdx.x];
-  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
-  if (s >= R->row_off + R->n) return;
-  const float4 pi = d.posf[s];
-  int cx, cy, cz;
-  cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cx, cy, cz);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SegTable& S = seg[wid];
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
   const float cut2 = warren ? R->wrd * R->wrd : 1.0f;
   const double cut2d = warren ? (double)R->wrd * (double)R->wrd : 1.0;
   const float inv_rd = R->winv_rd, wnorm = R->wnorm;
   const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
-  long long q0 = 0, q1 = 0, q2 = 0;
-  for_each_cell27(R, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
-    const int tb = d.cell_start[cn], te = d.cell_start[cn + 1];
-    const float bx = pi.x - (float)dx * csx, by = pi.y - (float)dy * csy,
-                bz = pi.z - (float)dz * csz;
-    for (int t = tb; t < te; t++) {
-      if (t == s) continue;
-      const float4 pj = __ldg(d.posf + t);
-      const float ex = bx - pj.x, ey = by - pj.y, ez = bz - pj.z;
-      const float dr2 = ex * ex + ey * ey + ez * ez;
-      if (dr2 < cut2 + kGuard) {
-        bool in = dr2 < cut2;
-        if (fabsf(dr2 - cut2) <= kGuard || dr2 < 1.0e-10f) {
-          const double e2 = exact_dr2(d, R, d.perm[s], d.perm[t], sx, sy, sz);
-          in = e2 < cut2d && e2 != 0.0;
-        }
-        if (in) {
-          const float dr = sqrtf(dr2);
-          float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
-          w = warren ? wnorm * (w * w) : w * w;
-          const long long v = to_fix(w, kDensScaleF);
-          const uint32_t pr = fbits(pj.w);
-          if (pr == 0) q0 += v;
-          else if (pr == 1) q1 += v;
-          else q2 += v;
+  const int nseg = 2 * (2 * R->reach + 1) * (2 * R->reach + 1);
+  int cached = -1;
+  for (int s = s0; s < s_end; s++) {
+    const int cell = (int)d.scell[s];
+    if (cell != cached) {
+      int cx, cy, cz;
+      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+      __syncwarp();
+      build_segments(S, d, R, cx, cy, cz, lane);
+      __syncwarp();
+      cached = cell;
+    }
+    const float4 pi = d.posf[s];
+    long long q0 = 0, q1 = 0, q2 = 0;
+    for (int g = 0; g < nseg; g++) {
+      const int tb = S.tb[g], te = S.te[g];
+      if (tb >= te) continue;
+      const int code = S.code[g];
+      const int dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
+      for (int t0 = tb; t0 < te; t0 += 32) {
+        const int t = t0 + lane;
+        if (t >= te || t == s) continue;
+        const float4 pj = __ldg(d.posf + t);
+        const int dx = seg_dx(S, g, t);
+        const float ex = (pi.x - (float)dx * csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
+        const float dr2 = ex * ex + ey * ey + ez * ez;
+        if (dr2 < cut2 + kGuard) {
+          bool in = dr2 < cut2;
+          if (fabsf(dr2 - cut2) <= kGuard || dr2 < 1.0e-10f) {
+            const PairCode pc = unpack_code(pack_code(dx, code));
+            const double e2 = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz);
+            in = e2 < cut2d && e2 != 0.0;
+          }
+          if (in) {
+            const float dr = sqrtf(dr2);
+            float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
+            w = warren ? wnorm * (w * w) : w * w;
+            const long long v = fix_from_float(w, kDensBits);
+            const uint32_t pr = fbits(pj.w);
+            q0 += pr == 0 ? v : 0ll;
+            q1 += pr == 1 ? v : 0ll;
+            q2 += pr == 2 ? v : 0ll;
+          }
         }
       }
     }
-  });
-  d.densf[s] = make_float4((float)((double)q0 * kDensUnscale), (float)((double)q1 * kDensUnscale),
-                           (float)((double)q2 * kDensUnscale), 0.0f);
-  if (d.dqx) {
-    d.dqx[s] = q0;
-    d.dqy[s] = q1;
-    d.dqz[s] = q2;
+    q0 = warp_sum_ll(q0);
+    q1 = warp_sum_ll(q1);
+    q2 = warp_sum_ll(q2);
+    if (lane == 0) {
+      d.densf[s] = make_float4(fix_to_float(q0, kDensUnscaleF), fix_to_float(q1, kDensUnscaleF),
+                               fix_to_float(q2, kDensUnscaleF), 0.0f);
+      if (d.dqx) {
+        d.dqx[s] = q0;
+        d.dqy[s] = q1;
+        d.dqz[s] = q2;
+      }
+    }
+  }
+}
+
+// Visits every neighbour cell within the stencil of the given reach
+// (plain FP64 kernels and the centre-of-mass pass).
+template <class F>
+__device__ __forceinline__ void for_each_cell(const RepDev* R, int reach, int cx, int cy, int cz,
+                                              F&& f) {
+  const int nx = R->nc[0], ny = R->nc[1], nz = R->nc[2];
+  for (int dz = -reach; dz <= reach; dz++) {
+    const int qz = cz + dz, sz = qz < 0 ? -1 : (qz >= nz ? 1 : 0), wz = qz - sz * nz;
+    for (int dy = -reach; dy <= reach; dy++) {
+      const int qy = cy + dy, sy = qy < 0 ? -1 : (qy >= ny ? 1 : 0), wy = qy - sy * ny;
+      const int row = R->cell_off + (wz * ny + wy) * nx;
+      for (int dx = -reach; dx <= reach; dx++) {
+        const int qx = cx + dx, sx = qx < 0 ? -1 : (qx >= nx ? 1 : 0), wx = qx - sx * nx;
+        f(row + wx, dx, dy, dz, sx, sy, sz);
+      }
+    }
   }
 }
 
@@ -114,20 +221,20 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   const int s = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
   if (s >= R->row_off + R->n) return;
+  const RepTab64* T = d.tab64 + r;
   const uint32_t i = d.perm[s];
   const double xi = d.px[i], yi = d.py[i], zi = d.pz[i];
   int cx, cy, cz;
   cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cx, cy, cz);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
-  const double rd = (double)R->wrd;
+  const double rd = T->wrd;
   const double cut2 = warren ? rd * rd : 1.0;
   const double wn = 15.0 / (2.0 * 3.14159265358979323846 * rd * rd * rd);
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for_each_cell27(R, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
-    const int tb = d.cell_start[cn], te = d.cell_start[cn + 1];
+  for_each_cell(R, R->reach, cx, cy, cz, [&](int cn, int, int, int, int sx, int sy, int sz) {
     const double shx = (double)sx * R->box[0], shy = (double)sy * R->box[1],
                  shz = (double)sz * R->box[2];
-    for (int t = tb; t < te; t++) {
+    for (int t = d.cell_start[cn]; t < d.cell_start[cn + 1]; t++) {
       const uint32_t j = d.perm[t];
       const double ex = xi - (d.px[j] + shx), ey = yi - (d.py[j] + shy), ez = zi - (d.pz[j] + shz);
       const double dr2 = ex * ex + ey * ey + ez * ez;
@@ -151,6 +258,11 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   d.dens64[3 * s + 1] = a1;
   d.dens64[3 * s + 2] = a2;
   d.densf[s] = make_float4((float)a0, (float)a1, (float)a2, 0.0f);
+  if (d.dqx) {
+    d.dqx[s] = __double2ll_rn(a0 * kDensScale);
+    d.dqy[s] = __double2ll_rn(a1 * kDensScale);
+    d.dqz[s] = __double2ll_rn(a2 * kDensScale);
+  }
 }
 
 void launch_density(const DevState& d, int nblk, bool fp64, cudaStream_t st) {
@@ -166,15 +278,13 @@ struct PairTables {
   float cf_c[9], cf_g[9], cf_r[9], cf_m[27];
 };
 
-// Conservative + random + dissipative magnitude over dr
-// (nbdf_calculator.hpp:108-132) for one pair, FP32.
+// Conservative + random + dissipative magnitude over dr for one pair
+// (nbdf_calculator.hpp:108-132), FP32. dr, 1/dr and w = 1 - dr are passed in.
 __device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* R, int form,
-                                             uint32_t pri, uint32_t prj, float dr2, float ex,
-                                             float ey, float ez, float4 vi, float4 vj, float4 di,
-                                             float4 dj, uint32_t idi, uint32_t idj, uint32_t seed) {
-  const float inv_dr = rsqrtf(dr2);
-  const float dr = dr2 * inv_dr;
-  const float w = 1.0f - dr;
+                                             uint32_t pri, uint32_t prj, float dr, float inv_dr,
+                                             float w, float ex, float ey, float ez, float4 vi,
+                                             float4 vj, float4 di, float4 dj, uint32_t idi,
+                                             uint32_t idj, uint32_t seed) {
   const float sqw = sqrtf(w);
   const int k = pri * 3 + prj;
   float cons;
@@ -196,14 +306,42 @@ __device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* 
   return (cons + T.cf_r[k] * sqw * rnd - T.cf_g[k] * w * ddv * inv_dr) * inv_dr;
 }
 
-// One thread per sorted slot. Phase A walks the 27 cells and writes the
-// in-range neighbours (sorted index | cell-offset code << 27) into a
-// per-thread column of shared memory; phase B evaluates the pairs of the
-// column with all lanes busy. A full column is evaluated before the walk
-// continues, so there is no neighbour limit.
+// Pairs with dr^2 above this take w = 1 - dr from the compensated path.
+constexpr float kNearCut2 = 0.98f;
+
+// 1 - dr for a pair close to the cutoff, from the double-float cell-local
+// coordinates (hi + lo) and the double-float cell side: every step below is
+// an error-free transform or acts on terms below 1e-7, so 1 - dr^2 carries
+// an absolute error near 1e-13 instead of the 1e-7 of the FP32 pair vector.
+// The random term's sqrt(1 - r) amplifies the latter when r is near 1.
+__device__ __forceinline__ float near_cut_w(float4 pi, float4 li, float4 pj, float4 lj, int dx,
+                                            int dy, int dz, const RepDev* R, float dr) {
+  const float hi_i[3] = {pi.x, pi.y, pi.z}, lo_i[3] = {li.x, li.y, li.z};
+  const float hi_j[3] = {pj.x, pj.y, pj.z}, lo_j[3] = {lj.x, lj.y, lj.z};
+  const int dk[3] = {dx, dy, dz};
+  float p[3], err = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float e1, e2, pe;
+    const float s = two_sum(hi_i[k], -hi_j[k], e1);
+    const float t = two_sum(s, -(float)dk[k] * R->cs_f[k], e2);
+    const float lo = e1 + e2 + (lo_i[k] - lo_j[k]) - (float)dk[k] * R->cs_lo[k];
+    p[k] = two_prod(t, t, pe);
+    err += pe + 2.0f * t * lo;
+  }
+  float ea, eb;
+  const float s1 = two_sum(p[0], p[1], ea);
+  const float s2 = two_sum(s1, p[2], eb);
+  const float w2 = (1.0f - s2) - (err + ea + eb);  // 1 - s2 is exact for s2 in [0.5, 2]
+  return w2 / (1.0f + dr);
+}
+
+// One warp per particle (see the file comment). The warp queue holds the
+// sorted index and the offset code of each in-range neighbour.
 template <bool PRESS>
-__global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d, int cap) {
-  extern __shared__ uint32_t lst[];
+__global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
+  __shared__ SegTable seg[kWarps];
+  __shared__ uint32_t qt[kWarps][64], qc[kWarps][64];
   __shared__ PairTables T;
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
@@ -216,95 +354,148 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d, int cap) {
     (&T.cf_c[0])[k] = v;
   }
   __syncthreads();
-  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
-  if (s >= R->row_off + R->n) return;
-  const int B = blockDim.x;
-  uint32_t* col = lst + threadIdx.x;
-  const float4 pi = d.posf[s];
-  const float4 vi = d.velf[s];
-  const float4 di = d.densf[s];
-  const uint32_t idi = fbits(vi.w), pri = fbits(pi.w);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SegTable& S = seg[wid];
+  uint32_t* QT = qt[wid];
+  uint32_t* QC = qc[wid];
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
   const uint32_t seed = R->seed + d.rep_time[r];
   const int form = R->form;
   const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
-  int cx, cy, cz;
-  cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cx, cy, cz);
-  long long fx = 0, fy = 0, fz = 0, px = 0, py = 0, pz = 0;
-
-  auto flush = [&](int cnt) {
-    for (int k = 0; k < cnt; k++) {
-      const uint32_t e = col[k * B];
-      const int t = (int)(e & 0x7ffffffu);
-      const int code = (int)(e >> 27);
-      const int dz = code / 9 - 1, dy = (code / 3) % 3 - 1, dx = code % 3 - 1;
-      const float4 vj = __ldg(d.velf + t);
-      const uint32_t idj = fbits(vj.w);
-      if (idj == idi) continue;
-      const float4 pj = __ldg(d.posf + t);
-      const float4 dj = __ldg(d.densf + t);
-      const float ex = (pi.x - (float)dx * csx) - pj.x;
-      const float ey = (pi.y - (float)dy * csy) - pj.y;
-      const float ez = (pi.z - (float)dz * csz) - pj.z;
-      const float dr2 = ex * ex + ey * ey + ez * ez;
-      const float a = pair_all_cf(T, R, form, pri, fbits(pj.w), dr2, ex, ey, ez, vi, vj, di, dj,
-                                  idi, idj, seed);
-      if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
-      const float gx = a * ex, gy = a * ey, gz = a * ez;
-      fx += to_fix(gx, kForceScaleF);
-      fy += to_fix(gy, kForceScaleF);
-      fz += to_fix(gz, kForceScaleF);
-      if (PRESS) {
-        px += to_fix(gx * ex, kForceScaleF);
-        py += to_fix(gy * ey, kForceScaleF);
-        pz += to_fix(gz * ez, kForceScaleF);
-      }
+  const int nseg = 2 * (2 * R->reach + 1) * (2 * R->reach + 1);
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  int cached = -1;
+  for (int s = s0; s < s_end; s++) {
+    const int cell = (int)d.scell[s];
+    if (cell != cached) {
+      int cx, cy, cz;
+      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+      __syncwarp();
+      build_segments(S, d, R, cx, cy, cz, lane);
+      __syncwarp();
+      cached = cell;
     }
-  };
+    const float4 pi = d.posf[s];
+    const float4 vi = d.velf[s];
+    const float4 di = d.densf[s];
+    const float4 li = d.poslo[s];
+    const uint32_t idi = fbits(vi.w), pri = fbits(pi.w);
+    long long fx = 0, fy = 0, fz = 0, px = 0, py = 0, pz = 0;
+    int qn = 0;
 
-  int cnt = 0;
-  for_each_cell27(R, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
-    const int tb = d.cell_start[cn], te = d.cell_start[cn + 1];
-    const float bx = pi.x - (float)dx * csx, by = pi.y - (float)dy * csy,
-                bz = pi.z - (float)dz * csz;
-    const uint32_t code = (uint32_t)((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)) << 27;
-    for (int t = tb; t < te; t++) {
-      if (t == s) continue;
-      const float4 pj = __ldg(d.posf + t);
-      const float ex = bx - pj.x, ey = by - pj.y, ez = bz - pj.z;
-      const float dr2 = ex * ex + ey * ey + ez * ez;
-      if (dr2 < 1.0f + kGuard) {
-        bool in = dr2 < 1.0f;
-        if (fabsf(dr2 - 1.0f) <= kGuard)
-          in = exact_dr2(d, R, d.perm[s], d.perm[t], sx, sy, sz) < 1.0;
-        if (in) {
-          col[cnt * B] = (uint32_t)t | code;
-          if (++cnt == cap) {
-            flush(cnt);
-            cnt = 0;
+    // evaluates queue entries [0, cnt) with lane k on entry k
+    auto evaluate = [&](int cnt) {
+      if (lane < cnt) {
+        const int t = (int)QT[lane];
+        const PairCode pc = unpack_code(QC[lane]);
+        const float4 vj = __ldg(d.velf + t);
+        const uint32_t idj = fbits(vj.w);
+        if (idj != idi) {
+          const float4 pj = __ldg(d.posf + t);
+          const float4 dj = __ldg(d.densf + t);
+          const float ex = (pi.x - (float)pc.dx * csx) - pj.x;
+          const float ey = (pi.y - (float)pc.dy * csy) - pj.y;
+          const float ez = (pi.z - (float)pc.dz * csz) - pj.z;
+          const float dr2 = ex * ex + ey * ey + ez * ez;
+          const float inv_dr = rsqrtf(dr2);
+          const float dr = dr2 * inv_dr;
+          float w = 1.0f - dr;
+          if (dr2 > kNearCut2)  // admitted pairs have 1 - r >= 0 up to ~1e-13
+            w = fmaxf(near_cut_w(pi, li, pj, __ldg(d.poslo + t), pc.dx, pc.dy, pc.dz, R, dr), 0.0f);
+          const float a = pair_all_cf(T, R, form, pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, vi,
+                                      vj, di, dj, idi, idj, seed);
+          if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
+          const float gx = a * ex, gy = a * ey, gz = a * ez;
+          fx += fix_from_float(gx, kForceBits);
+          fy += fix_from_float(gy, kForceBits);
+          fz += fix_from_float(gz, kForceBits);
+          if (PRESS) {
+            px += fix_from_float(gx * ex, kForceBits);
+            py += fix_from_float(gy * ey, kForceBits);
+            pz += fix_from_float(gz * ez, kForceBits);
           }
         }
       }
+    };
+
+    for (int g = 0; g < nseg; g++) {
+      const int tb = S.tb[g], te = S.te[g];
+      if (tb >= te) continue;
+      const int code = S.code[g];
+      const int dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
+      for (int t0 = tb; t0 < te; t0 += 32) {
+        const int t = t0 + lane;
+        bool in = false;
+        int dx = 0;
+        if (t < te && t != s) {
+          const float4 pj = __ldg(d.posf + t);
+          dx = seg_dx(S, g, t);
+          const float ex = (pi.x - (float)dx * csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
+          const float dr2 = ex * ex + ey * ey + ez * ez;
+          if (dr2 < 1.0f + kGuard) {
+            in = dr2 < 1.0f;
+            if (fabsf(dr2 - 1.0f) <= kGuard) {
+              const PairCode pc = unpack_code(pack_code(dx, code));
+              in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
+            }
+          }
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, in);
+        if (in) {
+          const int pos = qn + __popc(mask & lt_mask);
+          QT[pos] = (uint32_t)t;
+          QC[pos] = pack_code(dx, code);
+        }
+        qn += __popc(mask);
+        if (qn >= 32) {
+          __syncwarp();
+          evaluate(32);
+          __syncwarp();
+          if (lane < qn - 32) {
+            QT[lane] = QT[32 + lane];
+            QC[lane] = QC[32 + lane];
+          }
+          __syncwarp();
+          qn -= 32;
+        }
+      }
     }
-  });
-  flush(cnt);
-  d.fqx[s] = fx;
-  d.fqy[s] = fy;
-  d.fqz[s] = fz;
-  if (PRESS) {
-    d.pqx[s] = px;
-    d.pqy[s] = py;
-    d.pqz[s] = pz;
+    __syncwarp();
+    evaluate(qn);
+    __syncwarp();
+    fx = warp_sum_ll(fx);
+    fy = warp_sum_ll(fy);
+    fz = warp_sum_ll(fz);
+    if (PRESS) {
+      px = warp_sum_ll(px);
+      py = warp_sum_ll(py);
+      pz = warp_sum_ll(pz);
+    }
+    if (lane == 0) {
+      d.fqx[s] = fx;
+      d.fqy[s] = fy;
+      d.fqz[s] = fz;
+      if (PRESS) {
+        d.pqx[s] = px;
+        d.pqy[s] = py;
+        d.pqz[s] = pz;
+      }
+    }
   }
 }
 
 // Plain FP64 pass 2 (the FP64 baseline): the reference's arithmetic on the
-// FP64 rows, FP64 sums in cell order, stored as 2^-32 fixed point.
+// FP64 rows with the FP64 coefficient tables, FP64 sums in cell order,
+// stored in the engine's fixed point.
 template <bool PRESS>
 __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
   const int r = d.blk_rep[blockIdx.x];
   const int s = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
   if (s >= R->row_off + R->n) return;
+  const RepTab64* T = d.tab64 + r;
   const uint32_t i = d.perm[s];
   const double xi = d.px[i], yi = d.py[i], zi = d.pz[i];
   const double vxi = d.vx[i], vyi = d.vy[i], vzi = d.vz[i];
@@ -312,15 +503,14 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
   const double di0 = d.dens64[3 * s], di1 = d.dens64[3 * s + 1], di2 = d.dens64[3 * s + 2];
   const uint32_t seed = R->seed + d.rep_time[r];
   const int form = R->form;
-  const double rd = (double)R->wrd;
+  const double rd = T->wrd;
   int cx, cy, cz;
   cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cx, cy, cz);
   double f0 = 0.0, f1 = 0.0, f2 = 0.0, p0 = 0.0, p1 = 0.0, p2 = 0.0;
-  for_each_cell27(R, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
-    const int tb = d.cell_start[cn], te = d.cell_start[cn + 1];
+  for_each_cell(R, R->reach, cx, cy, cz, [&](int cn, int, int, int, int sx, int sy, int sz) {
     const double shx = (double)sx * R->box[0], shy = (double)sy * R->box[1],
                  shz = (double)sz * R->box[2];
-    for (int t = tb; t < te; t++) {
+    for (int t = d.cell_start[cn]; t < d.cell_start[cn + 1]; t++) {
       const uint32_t j = d.perm[t];
       if (d.id[j] == idi) continue;
       const double ex = xi - (d.px[j] + shx), ey = yi - (d.py[j] + shy), ez = zi - (d.pz[j] + shz);
@@ -341,16 +531,17 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
         } else if (form == IDPD_FORM_WARREN_K) {
           const double rho = (di0 + dj0) + (di1 + dj1) + (di2 + dj2);
           const double wb = dr < rd ? 1.0 - dr / rd : 0.0;
-          cons = (double)R->wa * w + (double)R->wb * rho * wb;
+          cons = T->wa * w + T->wb * rho * wb;
         } else {
-          const double cf_pair = dr >= kArcD ? (double)R->cf_c[k] * (dr - kArcD) : 0.0;
-          const double cf_mbd = (double)R->cf_m[3 * k] * (di0 + dj0) +
-                                (double)R->cf_m[3 * k + 1] * (di1 + dj1) +
-                                (double)R->cf_m[3 * k + 2] * (di2 + dj2);
+          const double cf_pair = T->cf_c[k] * (dr - kArcD) * (double)(dr >= kArcD);
+          double cf_mbd = 0.0;
+          cf_mbd += T->cf_m[3 * k] * (di0 + dj0);
+          cf_mbd += T->cf_m[3 * k + 1] * (di1 + dj1);
+          cf_mbd += T->cf_m[3 * k + 2] * (di2 + dj2);
           cons = (cf_pair + cf_mbd) * w;
         }
-        const double all = (cons + (double)R->cf_r[k] * sqrt(w) * rnd -
-                            (double)R->cf_g[k] * w * (ex * dvx + ey * dvy + ez * dvz) * inv_dr) *
+        const double all = (cons + T->cf_r[k] * sqrt(w) * rnd -
+                            T->cf_g[k] * w * (ex * dvx + ey * dvy + ez * dvz) * inv_dr) *
                            inv_dr;
         f0 += all * ex;
         f1 += all * ey;
@@ -375,6 +566,7 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
 
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st) {
+  (void)tu;
   if (nblk == 0) return;
   if (fp64) {
     if (with_press)
@@ -383,26 +575,25 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
       k_force_f64<false><<<nblk, kRowBlock, 0, st>>>(d);
     return;
   }
-  const size_t smem = (size_t)tu.list_cap * kRowBlock * sizeof(uint32_t);
   if (with_press)
-    k_force_f32<true><<<nblk, kRowBlock, smem, st>>>(d, tu.list_cap);
+    k_force_f32<true><<<nblk, kRowBlock, 0, st>>>(d);
   else
-    k_force_f32<false><<<nblk, kRowBlock, smem, st>>>(d, tu.list_cap);
+    k_force_f32<false><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // -------------------------------------------- neighbour centre of mass
 // The hydrophilic / hydrophobic neighbour sums of pass 1
 // (nbdf_calculator.hpp:23-51) and FPDPD::copyFromForce (ptcl_class.hpp:53-57),
-// for the fine-grained API and the chemistry: reach of two cells (radius
-// rn_c = 1.2), positions summed relative to the row's cell origin in 2^-40
-// fixed point, written per storage row.
+// for the fine-grained API and the chemistry: reach one more than the pair
+// stencil (radius rn_c = 1.2), positions summed relative to the row's cell
+// origin in 2^-40 fixed point, written per storage row.
 __global__ void __launch_bounds__(kRowBlock) k_com(DevState d, double* cm, uint32_t* cnt_out) {
   const int r = d.blk_rep[blockIdx.x];
   const int s = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
   if (s >= R->row_off + R->n) return;
-  const int nx = R->nc[0], ny = R->nc[1], nz = R->nc[2];
-  if (nx < 5 || ny < 5 || nz < 5) {
+  const int reach = R->reach + 1;
+  if (R->nc[0] < 2 * reach + 1 || R->nc[1] < 2 * reach + 1 || R->nc[2] < 2 * reach + 1) {
     atomicCAS(d.err, 0, kErrComBox);
     return;
   }
@@ -412,49 +603,42 @@ __global__ void __launch_bounds__(kRowBlock) k_com(DevState d, double* cm, uint3
   const float rn2 = 1.44f;
   const double rn2d = 1.2 * 1.2;
   // hydrophilic sum starts at the row itself with count 1 (nbdf_calculator.hpp:23-24)
-  long long hl[3] = {to_fix(pi.x, kPosScaleF), to_fix(pi.y, kPosScaleF), to_fix(pi.z, kPosScaleF)};
+  long long hl[3] = {fix_from_float(pi.x, kPosBits), fix_from_float(pi.y, kPosBits),
+                     fix_from_float(pi.z, kPosBits)};
   long long hb[3] = {0, 0, 0};
   uint32_t cl = 1, cb = 0;
   const uint32_t i = d.perm[s];
-  for (int dz = -2; dz <= 2; dz++) {
-    const int qz = cz + dz, sz = qz < 0 ? -1 : (qz >= nz ? 1 : 0), wz = qz - sz * nz;
-    for (int dy = -2; dy <= 2; dy++) {
-      const int qy = cy + dy, sy = qy < 0 ? -1 : (qy >= ny ? 1 : 0), wy = qy - sy * ny;
-      for (int dx = -2; dx <= 2; dx++) {
-        const int qx = cx + dx, sx = qx < 0 ? -1 : (qx >= nx ? 1 : 0), wx = qx - sx * nx;
-        const int cn = R->cell_off + (wz * ny + wy) * nx + wx;
-        const float ox = (float)dx * R->cs_f[0], oy = (float)dy * R->cs_f[1],
-                    oz = (float)dz * R->cs_f[2];
-        for (int t = d.cell_start[cn]; t < d.cell_start[cn + 1]; t++) {
-          if (t == s) continue;
-          const float4 pj = d.posf[t];
-          const float jx = pj.x + ox, jy = pj.y + oy, jz = pj.z + oz;
-          const float ex = pi.x - jx, ey = pi.y - jy, ez = pi.z - jz;
-          const float dr2 = ex * ex + ey * ey + ez * ez;
-          if (dr2 >= rn2 + kGuard) continue;
-          bool in_b = dr2 < rn2, in_l = dr2 < 1.0f;
-          if (fabsf(dr2 - rn2) <= kGuard || fabsf(dr2 - 1.0f) <= kGuard || dr2 < 1.0e-10f) {
-            const double e2 = exact_dr2(d, R, i, d.perm[t], sx, sy, sz);
-            in_b = e2 < rn2d && e2 != 0.0;
-            in_l = in_b && e2 < 1.0;
-          }
-          const uint32_t pr = fbits(pj.w);
-          if (in_b && pr == 1) {
-            hb[0] += to_fix(jx, kPosScaleF);
-            hb[1] += to_fix(jy, kPosScaleF);
-            hb[2] += to_fix(jz, kPosScaleF);
-            cb++;
-          }
-          if (in_l && pr == 0) {
-            hl[0] += to_fix(jx, kPosScaleF);
-            hl[1] += to_fix(jy, kPosScaleF);
-            hl[2] += to_fix(jz, kPosScaleF);
-            cl++;
-          }
-        }
+  for_each_cell(R, reach, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
+    const float ox = (float)dx * R->cs_f[0], oy = (float)dy * R->cs_f[1],
+                oz = (float)dz * R->cs_f[2];
+    for (int t = d.cell_start[cn]; t < d.cell_start[cn + 1]; t++) {
+      if (t == s) continue;
+      const float4 pj = d.posf[t];
+      const float jx = pj.x + ox, jy = pj.y + oy, jz = pj.z + oz;
+      const float ex = pi.x - jx, ey = pi.y - jy, ez = pi.z - jz;
+      const float dr2 = ex * ex + ey * ey + ez * ez;
+      if (dr2 >= rn2 + kGuard) continue;
+      bool in_b = dr2 < rn2, in_l = dr2 < 1.0f;
+      if (fabsf(dr2 - rn2) <= kGuard || fabsf(dr2 - 1.0f) <= kGuard || dr2 < 1.0e-10f) {
+        const double e2 = exact_dr2(d, R, i, d.perm[t], sx, sy, sz);
+        in_b = e2 < rn2d && e2 != 0.0;
+        in_l = in_b && e2 < 1.0;
+      }
+      const uint32_t pr = fbits(pj.w);
+      if (in_b && pr == 1) {
+        hb[0] += fix_from_float(jx, kPosBits);
+        hb[1] += fix_from_float(jy, kPosBits);
+        hb[2] += fix_from_float(jz, kPosBits);
+        cb++;
+      }
+      if (in_l && pr == 0) {
+        hl[0] += fix_from_float(jx, kPosBits);
+        hl[1] += fix_from_float(jy, kPosBits);
+        hl[2] += fix_from_float(jz, kPosBits);
+        cl++;
       }
     }
-  }
+  });
   const double org[3] = {(double)cx * R->cs[0], (double)cy * R->cs[1], (double)cz * R->cs[2]};
   for (int k = 0; k < 3; k++) {
     cm[6 * i + k] = org[k] + ((double)hl[k] / kPosScale) / (double)cl;

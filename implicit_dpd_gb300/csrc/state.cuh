@@ -37,6 +37,7 @@ struct DevState {
   uint32_t* rank;
   uint32_t* scell;
   float4 *posf, *velf, *densf;
+  float4* poslo;               // low-order parts of the cell-local position
   long long *fqx, *fqy, *fqz;  // pair force, 2^-32 fixed point
   long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API only)
   long long *dqx, *dqy, *dqz;  // partial densities, 2^-40 fixed point (fine-grained API only)
@@ -46,6 +47,7 @@ struct DevState {
   float* cf_bend;   // [total molecules]
   // ---- replicas and launch maps
   RepDev* reps;
+  RepTab64* tab64;
   uint32_t* rep_time;  // Parameter::time per replica
   int* blk_rep;
   int* blk_row;
@@ -72,8 +74,7 @@ void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
 
 // kernels_pairs.cu
 struct PairTuning {
-  int list_cap;    // neighbour slots per thread in shared memory
-  int block;       // threads per block (multiple of 32, <= kRowBlock)
+  int reach;       // 1: cells of the cutoff, 27-cell stencil; 2: half cells, 125-cell stencil
 };
 void launch_density(const DevState& d, int nblk, bool fp64, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,

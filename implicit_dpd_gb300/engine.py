@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from .abi import STATUS_NAMES, IdpdConfig, IdpdParams, IdpdRunParam
+from .abi import STATUS_NAMES, IdpdConfig, IdpdParams, IdpdRunParam, IdpdTuning
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
@@ -27,7 +27,7 @@ EXPORTS = [
     "idpd_download_aux", "idpd_build_topology", "idpd_drift", "idpd_density", "idpd_force",
     "idpd_bonded", "idpd_kick", "idpd_remove_cmdrift", "idpd_step", "idpd_sync",
     "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
-    "idpd_cell_order", "idpd_set_dynamics",
+    "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
 ]
 
 _lib = None
@@ -67,6 +67,8 @@ def load(path=LIB_PATH):
     L.idpd_saru_nrml_f32.argtypes = [C.c_int32, U, U, U, F]
     L.idpd_cell_order.argtypes = [H, C.c_int32, VP, VP]
     L.idpd_set_dynamics.argtypes = [H, C.c_int32, VP, VP, VP]
+    L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
+    L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     _lib = L
     return L
 
@@ -161,6 +163,14 @@ class Engine:
         """Fills caller-provided (n, 3) float64 arrays, e.g. pinned buffers."""
         self._ck(self.L.idpd_download_state(self.h, replica, _p(pos), _p(vel), _p(acc), None, None,
                                             None, None), "download_dynamics")
+
+    def set_tuning(self, reach):
+        self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach))), "set_tuning")
+
+    def get_tuning(self):
+        t = IdpdTuning()
+        self._ck(self.L.idpd_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t.reach
 
     def num_particles(self, replica=0):
         n = C.c_int32()

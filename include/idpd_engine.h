@@ -176,6 +176,16 @@ int idpd_step(idpd_handle* h, int32_t nsteps);
 /* Blocks until the handle's stream is idle; reports device-side errors. */
 int idpd_sync(idpd_handle* h);
 
+/* ---- tuning --------------------------------------------------------------- */
+/* Launch and cell-grid shape of the pair passes. Every choice gives the same
+ * results bit for bit (all pair sums are fixed point); only speed changes. */
+typedef struct idpd_tuning {
+  int32_t reach;        /* 1: cells >= rc, 27-cell stencil; 2: cells >= rc/2, 125 cells */
+  int32_t reserved[7];
+} idpd_tuning;
+int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t);
+int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t);
+
 /* ---- timing -------------------------------------------------------------- */
 /* Elapsed milliseconds of the last idpd_step call measured with CUDA events
  * on the handle's stream. */

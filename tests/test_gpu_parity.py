@@ -244,3 +244,39 @@ def test_replicas_batched_equal_single_runs_bit_for_bit():
         a, b_ = eb.download(k), es.download()
         for key in ("pos", "vel", "acc", "id"):
             assert np.array_equal(a[key], b_[key]), (k, key)
+
+
+def test_cell_reach_gives_bit_identical_trajectories():
+    """Half-size cells (125-cell stencil) and cutoff-size cells (27 cells)
+    visit the same pairs; the fixed-point sums make the states identical."""
+    box, st, n_amp = mixed_system(seed=4)
+    p = mdpd_params(box, time=98)
+    out = []
+    for reach in (1, 2):
+        e = engine_for(p, st, n_amp, [1])
+        e.set_tuning(reach)
+        assert e.get_tuning() == reach
+        e.step(6)
+        out.append(e.download())
+    for key in ("pos", "vel", "acc"):
+        assert np.array_equal(out[0][key], out[1][key]), key
+
+
+def test_dense_membrane_density_force_match_oracle():
+    """The compacted membrane regime (~150 neighbours per bead) exercises the
+    pair queue far beyond one warp's worth of neighbours."""
+    box = np.array([7.0, 7.0, 5.0])
+    rng = np.random.default_rng(12)
+    st = configs.liquid(box, 30.0, seed=12, prop=1)
+    st["prop"] = rng.integers(0, 3, len(st["pos"])).astype(np.uint32)
+    p = mdpd_params(box, time=3)
+    dens, cm, cnt, acc, press = oracle_forces(p, st)
+    for reach in (1, 2):
+        e = engine_for(p, st)
+        e.set_tuning(reach)
+        e.density()
+        d = e.download_aux(density=True)
+        assert np.abs(d["dens"] - dens).max() / np.abs(dens).max() < FORCE_TOL
+        e.force()
+        worst, agg = rel_force_err(e.download()["acc"], acc)
+        assert worst < FORCE_TOL, (reach, worst, agg)
