@@ -43,11 +43,13 @@ constexpr float kGuard = 8.0e-6f;
 struct RepDev {
   double box[3];
   double ibox[3];    // 1 / box (Parameter::ibox_leng)
-  double inv_cs[3];  // cells per unit length (nc / box)
-  double cs[3];      // cell side (box / nc)
-  float cs_f[3];     // cell side rounded to float
+  double inv_cs[3];  // search cells per unit length (nc / box)
+  double cs[3];      // frame cell side (box / nf): cell-local coordinates refer to it
+  float cs_f[3];     // frame cell side rounded to float
   float cs_lo[3];    // cs - cs_f
-  int nc[3];
+  int nc[3];         // search cells per axis (reach * nf)
+  int nf[3];         // frame cells per axis (floor(box), side >= the cutoff)
+  int rshift;        // log2(reach): search cell c lies in frame cell c >> rshift
   int cell_off;      // first global cell of the replica
   int ncell;
   int row_off;       // first row (storage and sorted) of the replica

@@ -140,14 +140,19 @@ int check_params(idpd_handle* h, const idpd_params* p) {
   return IDPD_OK;
 }
 
+// Frame cells have side >= the cutoff (nf = floor(box)); the search grid
+// splits each frame cell into `reach` cells per axis. Positions are stored
+// relative to frame cells, so the search grid never changes a pair term.
 void fill_repdev(RepDev& R, const idpd_params& p, int reach) {
   R.reach = reach;
+  R.rshift = reach == 2 ? 1 : 0;
   for (int k = 0; k < 3; k++) {
     R.box[k] = p.box[k];
     R.ibox[k] = 1.0 / p.box[k];
-    R.nc[k] = (int)(p.box[k] * (double)reach);
+    R.nf[k] = (int)(p.box[k] / 1.0);
+    R.nc[k] = R.nf[k] * reach;
     R.inv_cs[k] = (double)R.nc[k] / p.box[k];
-    R.cs[k] = p.box[k] / (double)R.nc[k];
+    R.cs[k] = p.box[k] / (double)R.nf[k];
     R.cs_f[k] = (float)R.cs[k];
     R.cs_lo[k] = (float)(R.cs[k] - (double)R.cs_f[k]);
   }

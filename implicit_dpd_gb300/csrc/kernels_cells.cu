@@ -192,6 +192,9 @@ __global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
   d.scell[s] = key;
   int cx, cy, cz;
   cell_xyz((int)key - R->cell_off, R->nc, cx, cy, cz);
+  cx >>= R->rshift;  // frame cell
+  cy >>= R->rshift;
+  cz >>= R->rshift;
   // x - cx cs is exact in FP64 (Sterbenz: x lies in [o, 2o] or o = 0); its
   // float split keeps 48 bits for the near-cutoff pair terms.
   float lx, ly, lz, ex, ey, ez;

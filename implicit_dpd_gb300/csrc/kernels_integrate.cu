@@ -8,18 +8,19 @@
 
 namespace idpd {
 
-// Position of sorted slot t relative to the origin of cell (cx, cy, cz) of
-// the same replica, in FP32: cell-local coordinate plus the minimum-image
-// cell difference.
+// Position of sorted slot t relative to the origin of the frame cell that
+// holds search cell (cx, cy, cz) of the same replica, in FP32: frame-local
+// coordinate plus the minimum-image frame-cell difference.
 __device__ __forceinline__ float3 rel_pos(const DevState& d, const RepDev* R, int t, int cx, int cy,
                                           int cz) {
   const float4 p = d.posf[t];
   int tx, ty, tz;
   cell_xyz((int)d.scell[t] - R->cell_off, R->nc, tx, ty, tz);
-  int q[3] = {tx - cx, ty - cy, tz - cz};
+  const int rs = R->rshift;
+  int q[3] = {(tx >> rs) - (cx >> rs), (ty >> rs) - (cy >> rs), (tz >> rs) - (cz >> rs)};
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const int n = R->nc[k];
+    const int n = R->nf[k];
     if (2 * q[k] > n) q[k] -= n;
     if (2 * q[k] < -n) q[k] += n;
   }
@@ -208,23 +209,26 @@ void launch_fq_to_acc(const DevState& d, int nblk, double* press_out, cudaStream
 
 // ------------------------------------------------- centre-of-mass drift
 // Runs every step; a replica takes part only when its time is a multiple
-// of cm_corr (src/main.cpp:184) or when forced. Block sums are combined per
-// replica in block order, so the mean is deterministic.
+// of cm_corr (src/main.cpp:184) or when forced. Velocities are summed as
+// 2^-28 fixed-point integers, so the mean does not depend on the storage
+// order of the rows (which follows the cell grid).
+constexpr double kVelScale = 268435456.0;  // 2^28
+
 __device__ __forceinline__ bool cm_due(const DevState& d, int r, int force_now) {
   return force_now || (d.rep_time[r] % kCmCorr) == 0;
 }
 
 __global__ void __launch_bounds__(kRowBlock) k_cm_partial(DevState d, int force_now) {
-  __shared__ double sh[3][kRowBlock / 32];
+  __shared__ long long sh[3][kRowBlock / 32];
   const int r = d.blk_rep[blockIdx.x];
   if (!cm_due(d, r, force_now)) return;
   const int i = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
-  double v[3] = {0.0, 0.0, 0.0};
+  long long v[3] = {0, 0, 0};
   if (i < R->row_off + R->n) {
-    v[0] = d.vx[i];
-    v[1] = d.vy[i];
-    v[2] = d.vz[i];
+    v[0] = __double2ll_rn(d.vx[i] * kVelScale);
+    v[1] = __double2ll_rn(d.vy[i] * kVelScale);
+    v[2] = __double2ll_rn(d.vz[i] * kVelScale);
   }
 #pragma unroll
   for (int k = 0; k < 3; k++)
@@ -235,9 +239,9 @@ __global__ void __launch_bounds__(kRowBlock) k_cm_partial(DevState d, int force_
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int k = 0; k < 3; k++) {
-      double t = 0.0;
+      long long t = 0;
       for (int q = 0; q < kRowBlock / 32; q++) t += sh[k][q];
-      d.blk_part[3 * blockIdx.x + k] = t;
+      reinterpret_cast<long long*>(d.blk_part)[3 * blockIdx.x + k] = t;
     }
   }
 }
@@ -247,10 +251,11 @@ __global__ void k_cm_finalize(DevState d, int R_n, int force_now) {
   if (r >= R_n) return;
   if (!cm_due(d, r, force_now)) return;
   const RepDev* R = d.reps + r;
-  double s[3] = {0.0, 0.0, 0.0};
+  const long long* part = reinterpret_cast<const long long*>(d.blk_part);
+  long long s[3] = {0, 0, 0};
   for (int b = R->blk_off; b < R->blk_off + R->nblk; b++)
-    for (int k = 0; k < 3; k++) s[k] += d.blk_part[3 * b + k];
-  for (int k = 0; k < 3; k++) d.rep_mean[3 * r + k] = s[k] / (double)R->n;
+    for (int k = 0; k < 3; k++) s[k] += part[3 * b + k];
+  for (int k = 0; k < 3; k++) d.rep_mean[3 * r + k] = ((double)s[k] / kVelScale) / (double)R->n;
 }
 
 __global__ void __launch_bounds__(kRowBlock) k_cm_apply(DevState d, int force_now) {

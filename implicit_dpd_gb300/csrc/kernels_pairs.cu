@@ -38,30 +38,32 @@ __device__ __forceinline__ double exact_dr2(const DevState& d, const RepDev* R, 
 }
 
 // ------------------------------------------------ neighbour segments
-// A segment is a run of x-consecutive cells of one (dy, dz) row with one
-// image shift; its rows are contiguous in sorted order. Interior cell
-// boundaries give each candidate its x-cell offset.
+// A segment is a run of x-consecutive search cells of one (dy, dz) row with
+// one image shift; its rows are contiguous in sorted order. The boundaries
+// where the run enters a new frame cell give each candidate its x offset in
+// frame cells (the unit of the stored cell-local coordinates).
 constexpr int kMaxReach = 2;
 constexpr int kMaxSeg = 2 * (2 * kMaxReach + 1) * (2 * kMaxReach + 1);  // 50
 constexpr int kWarps = kRowBlock / 32;
 
 struct SegTable {
   int tb[kMaxSeg], te[kMaxSeg];
-  int bnd[kMaxSeg][2 * kMaxReach];  // start of the 2nd.. cells (INT_MAX when absent)
-  int code[kMaxSeg];                // dx0+4 | (dy+4)<<3 | (dz+4)<<6 | (sx+1)<<9 | (sy+1)<<11 | (sz+1)<<13
+  int bnd[kMaxSeg][2 * kMaxReach];  // first rows of the next frame cells (INT_MAX when absent)
+  int code[kMaxSeg];  // frame offsets fx0+4 | (fy+4)<<3 | (fz+4)<<6, shifts (sx+1)<<9 | (sy+1)<<11 | (sz+1)<<13
 };
 
 // Lane k < (2m+1)^2 builds the (up to two) segments of row k of cell
 // (cx, cy, cz); slots of a row that do not exist are left empty.
 __device__ __forceinline__ void build_segments(SegTable& S, const DevState& d, const RepDev* R,
                                                int cx, int cy, int cz, int lane) {
-  const int m = R->reach, w = 2 * m + 1;
+  const int m = R->reach, w = 2 * m + 1, rs = R->rshift;
   const int nx = R->nc[0], ny = R->nc[1], nz = R->nc[2];
   for (int k = lane; k < w * w; k += 32) {
     const int dz = k / w - m, dy = k % w - m;
     const int qz = cz + dz, sz = qz < 0 ? -1 : (qz >= nz ? 1 : 0), wz = qz - sz * nz;
     const int qy = cy + dy, sy = qy < 0 ? -1 : (qy >= ny ? 1 : 0), wy = qy - sy * ny;
     const int base = R->cell_off + (wz * ny + wy) * nx;
+    const int fy = (qy >> rs) - (cy >> rs), fz = (qz >> rs) - (cz >> rs);  // frame offsets
     // parts: [cx-m, -1] wrapped left (sx=-1), [max(cx-m,0), min(cx+m,nx-1)] (sx=0),
     // [nx, cx+m] wrapped right (sx=+1); at most two are non-empty.
     int slot = 2 * k;
@@ -82,10 +84,12 @@ __device__ __forceinline__ void build_segments(SegTable& S, const DevState& d, c
       const int ncells = hi - lo + 1;
       S.tb[slot] = d.cell_start[base + xs];
       S.te[slot] = d.cell_start[base + xs + ncells];
-#pragma unroll
-      for (int q = 0; q < 2 * kMaxReach; q++)
-        S.bnd[slot][q] = q + 1 < ncells ? d.cell_start[base + xs + q + 1] : 0x7fffffff;
-      S.code[slot] = (lo + 4) | ((dy + 4) << 3) | ((dz + 4) << 6) | ((part + 1) << 9) |
+      int nb = 0;
+      for (int q = 1; q < ncells; q++)  // unwrapped search cell cx+lo+q starts a frame cell
+        if (((cx + lo + q) & (m - 1)) == 0) S.bnd[slot][nb++] = d.cell_start[base + xs + q];
+      for (; nb < 2 * kMaxReach; nb++) S.bnd[slot][nb] = 0x7fffffff;
+      const int fx0 = ((cx + lo) >> rs) - (cx >> rs);
+      S.code[slot] = (fx0 + 4) | ((fy + 4) << 3) | ((fz + 4) << 6) | ((part + 1) << 9) |
                      ((sy + 1) << 11) | ((sz + 1) << 13);
       slot++;
     }
@@ -608,9 +612,13 @@ __global__ void __launch_bounds__(kRowBlock) k_com(DevState d, double* cm, uint3
   long long hb[3] = {0, 0, 0};
   uint32_t cl = 1, cb = 0;
   const uint32_t i = d.perm[s];
+  const int rs = R->rshift;
   for_each_cell(R, reach, cx, cy, cz, [&](int cn, int dx, int dy, int dz, int sx, int sy, int sz) {
-    const float ox = (float)dx * R->cs_f[0], oy = (float)dy * R->cs_f[1],
-                oz = (float)dz * R->cs_f[2];
+    // frame-cell offsets of the neighbour search cell
+    const int fx = ((cx + dx) >> rs) - (cx >> rs), fy = ((cy + dy) >> rs) - (cy >> rs),
+              fz = ((cz + dz) >> rs) - (cz >> rs);
+    const float ox = (float)fx * R->cs_f[0], oy = (float)fy * R->cs_f[1],
+                oz = (float)fz * R->cs_f[2];
     for (int t = d.cell_start[cn]; t < d.cell_start[cn + 1]; t++) {
       if (t == s) continue;
       const float4 pj = d.posf[t];
@@ -639,7 +647,8 @@ __global__ void __launch_bounds__(kRowBlock) k_com(DevState d, double* cm, uint3
       }
     }
   });
-  const double org[3] = {(double)cx * R->cs[0], (double)cy * R->cs[1], (double)cz * R->cs[2]};
+  const double org[3] = {(double)(cx >> rs) * R->cs[0], (double)(cy >> rs) * R->cs[1],
+                         (double)(cz >> rs) * R->cs[2]};
   for (int k = 0; k < 3; k++) {
     cm[6 * i + k] = org[k] + ((double)hl[k] / kPosScale) / (double)cl;
     cm[6 * i + 3 + k] = org[k] + ((double)hb[k] / kPosScale) / (double)cb;

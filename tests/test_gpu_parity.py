@@ -176,7 +176,7 @@ def test_remove_cmdrift():
     O.remove_cmdrift(vel)
     e = engine_for(p, st)
     e.remove_cmdrift()
-    assert np.abs(e.download()["vel"] - vel).max() < 1e-13
+    assert np.abs(e.download()["vel"] - vel).max() < 1e-8  # mean in 2^-28 fixed point
 
 
 def _step_compare(p, st, n_amp, core, nsteps):
