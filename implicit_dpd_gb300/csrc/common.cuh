@@ -20,15 +20,14 @@ constexpr int IDPD_FORM_PAIRWISE_K = 1;
 constexpr int IDPD_FORM_WARREN_K = 2;
 
 // Fixed-point scales of the order-independent accumulators.
-constexpr double kForceScale = 4294967296.0;         // 2^32 per unit force
-constexpr double kForceUnscale = 1.0 / 4294967296.0;
-constexpr float kForceScaleF = 4294967296.0f;
+constexpr double kForceScale = 67108864.0;           // 2^26 per unit force
+constexpr double kForceUnscale = 1.0 / 67108864.0;
 constexpr double kDensScale = 1099511627776.0;        // 2^40 per unit density
 constexpr float kDensScaleF = 1099511627776.0f;
 constexpr double kDensUnscale = 1.0 / 1099511627776.0;
 constexpr double kPosScale = 1099511627776.0;         // 2^40: COM sums, delta_sumr
 constexpr float kPosScaleF = 1099511627776.0f;
-constexpr int kForceBits = 32;
+constexpr int kForceBits = 26;
 constexpr int kDensBits = 40;
 constexpr int kPosBits = 40;
 constexpr float kDensUnscaleF = 1.0f / 1099511627776.0f;
@@ -65,6 +64,9 @@ struct RepDev {
   int n_amp;         // molecules of the replica
   int amp_off;       // first molecule slot in the global topology
   int reach;         // cells per cutoff: cell side >= 1 / reach, stencil (2 reach + 1)^3
+  float dens_prescale;    // 2^-k with every density weight * 2^-k <= 1
+  float dens_unscale_f;   // 2^(k - 23): one unit of the density fixed point
+  double dens_unscale;
 };
 
 // FP64 coefficient tables of a replica (plain FP64 kernels).
@@ -198,6 +200,20 @@ __device__ __forceinline__ float fix_to_float(long long q, float unscale) {
   const float hi = (float)(int)(q >> 32) * 4294967296.0f;
   const float lo = (float)(uint32_t)(q & 0xffffffffll);
   return (hi + lo) * unscale;
+}
+
+// round(v * 2^26) as int64 for |v| < 2^16 from two float roundings: the
+// mantissa of 1.5 * 2^23 + v 2^5 holds round(v 2^5) (hi); the remainder
+// v - hi 2^-5 is exact and |.| <= 2^-6, so a second rounding gives the low
+// 21 bits. Larger |v| take the bit-level path. Ties round to even.
+__device__ __forceinline__ long long fix_force(float v) {
+  if (!(fabsf(v) < 65536.0f)) return fix_from_float(v, kForceBits);
+  const float magic = 12582912.0f;  // 1.5 * 2^23
+  const float a = fmaf(v, 32.0f, magic);
+  const int hi = __float_as_int(a) - __float_as_int(magic);
+  const float r = fmaf(-(a - magic), 0.03125f, v);
+  const int lo = __float_as_int(fmaf(r, 67108864.0f, magic)) - __float_as_int(magic);
+  return ((long long)hi << 21) + (long long)lo;
 }
 
 // Fixed-point sum to double, exactly for |q| < 2^51: the integer is added

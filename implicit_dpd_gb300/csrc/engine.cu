@@ -174,6 +174,13 @@ void fill_repdev(RepDev& R, const idpd_params& p, int reach) {
   R.cf_s = (float)p.cf_s;
   R.seed = p.seed;
   R.form = p.form;
+  // density weights reach (1-r)^2 <= 1, or wnorm (1 - r/rd)^2 <= wnorm (Warren)
+  int k = 0;
+  const double wmax = p.form == IDPD_FORM_WARREN ? (double)R.wnorm : 1.0;
+  while (std::ldexp(1.0, k) < wmax) k++;
+  R.dens_prescale = (float)std::ldexp(1.0, -k);
+  R.dens_unscale = std::ldexp(1.0, k - 23);
+  R.dens_unscale_f = (float)R.dens_unscale;
 }
 
 // Allocates (or grows) every device array for the current layout.
@@ -208,6 +215,7 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.perm, cap); AL(d.rank, cap); AL(d.scell, cap);
   AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap); AL(d.poslo, cap);
   AL(d.fqx, cap); AL(d.fqy, cap); AL(d.fqz, cap);
+  AL(d.nbl, (size_t)kNbrCap * cap); AL(d.nbn, cap);
   AL(d.topol, 4 * ac);
   AL(d.cf_bend, ac);
   AL(d.reps, h->R);
@@ -449,7 +457,7 @@ void enqueue_step(idpd_handle* h) {
   launch_drift_bin(d, h->nblk, true, h->st);
   launch_scan(d, h->ncell_tot, h->n_tot, h->st);
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
-  launch_density(d, h->nblk, fp64, h->st);
+  launch_density(d, h->nblk, fp64, h->tune.reach, h->st);
   launch_force(d, h->nblk, fp64, false, h->tune, h->st);
   launch_bonded_kick(d, h->nblk, true, h->st);
   launch_cmdrift(d, h->nblk, h->R, false, h->st);
@@ -825,7 +833,7 @@ int idpd_download_aux(idpd_handle* h, int32_t r, double* density, double* press,
     std::vector<double> byrow(3 * (size_t)n);
     for (int sidx = 0; sidx < n; sidx++) {
       const int row = (int)perm[sidx] - R.row_off;
-      for (int k = 0; k < 3; k++) byrow[3 * (size_t)row + k] = (double)q[k][sidx] * kDensUnscale;
+      for (int k = 0; k < 3; k++) byrow[3 * (size_t)row + k] = (double)q[k][sidx] * R.dens_unscale;
     }
     scatter3(byrow, density, 3);
   }
@@ -878,7 +886,7 @@ int idpd_density(idpd_handle* h) {
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   enqueue_cells(h, false);
-  launch_density(h->d, h->nblk, fp64, h->st);
+  launch_density(h->d, h->nblk, fp64, h->tune.reach, h->st);
   launch_com(h->d, h->nblk, h->cm64, h->cm_cnt, h->st);
   h->density_valid = true;
   return check_device_error(h);
@@ -1020,7 +1028,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
   CK(cudaEventRecord(ev[3], h->st));
-  launch_density(h->d, h->nblk, fp64, h->st);
+  launch_density(h->d, h->nblk, fp64, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
   launch_force(h->d, h->nblk, fp64, false, h->tune, h->st);
   CK(cudaEventRecord(ev[5], h->st));

@@ -104,9 +104,9 @@ __global__ void __launch_bounds__(kRowBlock) k_bonded_kick(DevState d) {
 #pragma unroll
     for (int k = 1; k < 4; k++)
       if (k == u) fu = F[k];
-    f[0] += fix_from_float(fu.x, kForceBits);
-    f[1] += fix_from_float(fu.y, kForceBits);
-    f[2] += fix_from_float(fu.z, kForceBits);
+    f[0] += fix_force(fu.x);
+    f[1] += fix_force(fu.y);
+    f[2] += fix_force(fu.z);
   }
   const double acx = fix_to_double(f[0], kForceUnscale), acy = fix_to_double(f[1], kForceUnscale),
                acz = fix_to_double(f[2], kForceUnscale);

@@ -125,6 +125,28 @@ __device__ __forceinline__ PairCode unpack_code(uint32_t c) {
 }
 
 // ------------------------------------------------------------- pass 1
+// In-range neighbour list entry: segment slot g (6 bits), frame offset of the
+// candidate's cell relative to the segment's first frame cell (2 bits), row
+// within the segment (8 bits). kNbrFallback marks a particle whose list did
+// not fit (pass 2 then walks its cells again).
+constexpr uint32_t kNbrFallback = 0xffffu;
+
+__device__ __forceinline__ uint16_t nbr_entry(int g, int ddx, int off) {
+  return (uint16_t)(g | (ddx << 6) | (off << 8));
+}
+
+template <int REACH>
+__device__ __forceinline__ int frame_step(int t, const int* b) {
+  int k = 0;
+#pragma unroll
+  for (int q = 0; q < 2 * REACH; q++) k += t >= b[q];
+  return k;
+}
+
+// One warp per particle: partial densities (FP32 pair weights summed as
+// fixed-point integers, see the file comment) and the list of neighbours
+// within the pair cutoff that pass 2 evaluates.
+template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   const int r = d.blk_rep[blockIdx.x];
@@ -134,11 +156,12 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
-  const float cut2 = warren ? R->wrd * R->wrd : 1.0f;
-  const double cut2d = warren ? (double)R->wrd * (double)R->wrd : 1.0;
-  const float inv_rd = R->winv_rd, wnorm = R->wnorm;
+  const float cutd2 = R->wrd * R->wrd;  // density cutoff^2 (1 unless Warren)
+  const double cutd2d = (double)R->wrd * (double)R->wrd;
+  const float inv_rd = R->winv_rd, wnorm = R->wnorm, pre = R->dens_prescale;
   const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
-  const int nseg = 2 * (2 * R->reach + 1) * (2 * R->reach + 1);
+  constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
+  const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
   for (int s = s0; s < s_end; s++) {
     const int cell = (int)d.scell[s];
@@ -151,50 +174,80 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       cached = cell;
     }
     const float4 pi = d.posf[s];
-    long long q0 = 0, q1 = 0, q2 = 0;
+    uint16_t* list = d.nbl + (size_t)s * kNbrCap;
+    uint32_t q0 = 0, q1 = 0, q2 = 0;
+    int nl = 0;
+    bool lost = false;
+#pragma unroll 1
     for (int g = 0; g < nseg; g++) {
       const int tb = S.tb[g], te = S.te[g];
       if (tb >= te) continue;
       const int code = S.code[g];
-      const int dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+      int b[2 * REACH];
+#pragma unroll
+      for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+      const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
       const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
       for (int t0 = tb; t0 < te; t0 += 32) {
         const int t = t0 + lane;
-        if (t >= te || t == s) continue;
-        const float4 pj = __ldg(d.posf + t);
-        const int dx = seg_dx(S, g, t);
-        const float ex = (pi.x - (float)dx * csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
-        const float dr2 = ex * ex + ey * ey + ez * ez;
-        if (dr2 < cut2 + kGuard) {
-          bool in = dr2 < cut2;
-          if (fabsf(dr2 - cut2) <= kGuard || dr2 < 1.0e-10f) {
-            const PairCode pc = unpack_code(pack_code(dx, code));
-            const double e2 = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz);
-            in = e2 < cut2d && e2 != 0.0;
-          }
-          if (in) {
-            const float dr = sqrtf(dr2);
-            float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
-            w = warren ? wnorm * (w * w) : w * w;
-            const long long v = fix_from_float(w, kDensBits);
-            const uint32_t pr = fbits(pj.w);
-            q0 += pr == 0 ? v : 0ll;
-            q1 += pr == 1 ? v : 0ll;
-            q2 += pr == 2 ? v : 0ll;
+        bool in1 = false;  // within the pair cutoff 1
+        int ddx = 0;
+        if (t < te && t != s) {
+          const float4 pj = __ldg(d.posf + t);
+          ddx = frame_step<REACH>(t, b);
+          const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
+                      ez = bz - pj.z;
+          const float dr2 = ex * ex + ey * ey + ez * ez;
+          if (dr2 < 1.0f + kGuard) {
+            in1 = dr2 < 1.0f;
+            bool ind = dr2 < cutd2 && dr2 >= 1.0e-10f;  // density weight taken
+            const bool near1 = fabsf(dr2 - 1.0f) <= kGuard;
+            const bool neard = warren ? fabsf(dr2 - cutd2) <= kGuard : near1;
+            if (near1 || neard || dr2 < 1.0e-10f) {
+              const PairCode pc = unpack_code(pack_code(fx0 + ddx, code));
+              const double e2 = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz);
+              in1 = e2 < 1.0;
+              ind = e2 < cutd2d && e2 != 0.0;
+            }
+            if (ind) {
+              const float dr = sqrtf(dr2);
+              float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
+              w = warren ? wnorm * (w * w) : w * w;
+              // round(w * pre * 2^23) from the mantissa of 1 + w * pre, w * pre in [0, 1]
+              const uint32_t v = (uint32_t)(__float_as_int(fmaf(w, pre, 1.0f)) - 0x3f800000);
+              const uint32_t pr = fbits(pj.w);
+              q0 += pr == 0 ? v : 0u;
+              q1 += pr == 1 ? v : 0u;
+              q2 += pr == 2 ? v : 0u;
+            }
           }
         }
+        const uint32_t mask = __ballot_sync(0xffffffffu, in1);
+        const int off = t - tb;
+        if (in1) {
+          const int pos = nl + __popc(mask & lt_mask);
+          if (pos < kNbrCap) list[pos] = nbr_entry(g, ddx, off);
+        }
+        lost |= __any_sync(0xffffffffu, in1 && off > 255);
+        nl += __popc(mask);
       }
     }
-    q0 = warp_sum_ll(q0);
-    q1 = warp_sum_ll(q1);
-    q2 = warp_sum_ll(q2);
+    unsigned long long a0 = q0, a1 = q1, a2 = q2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
     if (lane == 0) {
-      d.densf[s] = make_float4(fix_to_float(q0, kDensUnscaleF), fix_to_float(q1, kDensUnscaleF),
-                               fix_to_float(q2, kDensUnscaleF), 0.0f);
+      const float u = R->dens_unscale_f;
+      d.densf[s] = make_float4(fix_to_float((long long)a0, u), fix_to_float((long long)a1, u),
+                               fix_to_float((long long)a2, u), 0.0f);
+      d.nbn[s] = (nl > kNbrCap || lost) ? (uint16_t)kNbrFallback : (uint16_t)nl;
       if (d.dqx) {
-        d.dqx[s] = q0;
-        d.dqy[s] = q1;
-        d.dqz[s] = q2;
+        d.dqx[s] = (long long)a0;
+        d.dqy[s] = (long long)a1;
+        d.dqz[s] = (long long)a2;
       }
     }
   }
@@ -263,18 +316,20 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   d.dens64[3 * s + 2] = a2;
   d.densf[s] = make_float4((float)a0, (float)a1, (float)a2, 0.0f);
   if (d.dqx) {
-    d.dqx[s] = __double2ll_rn(a0 * kDensScale);
-    d.dqy[s] = __double2ll_rn(a1 * kDensScale);
-    d.dqz[s] = __double2ll_rn(a2 * kDensScale);
+    d.dqx[s] = __double2ll_rn(a0 / R->dens_unscale);
+    d.dqy[s] = __double2ll_rn(a1 / R->dens_unscale);
+    d.dqz[s] = __double2ll_rn(a2 / R->dens_unscale);
   }
 }
 
-void launch_density(const DevState& d, int nblk, bool fp64, cudaStream_t st) {
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, cudaStream_t st) {
   if (nblk == 0) return;
   if (fp64)
     k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
+  else if (reach == 2)
+    k_density_f32<2><<<nblk, kRowBlock, 0, st>>>(d);
   else
-    k_density_f32<<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<1><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // ------------------------------------------------------------- pass 2
@@ -340,9 +395,51 @@ __device__ __forceinline__ float near_cut_w(float4 pi, float4 li, float4 pj, flo
   return w2 / (1.0f + dr);
 }
 
-// One warp per particle (see the file comment). The warp queue holds the
-// sorted index and the offset code of each in-range neighbour.
+// The particle of one warp in pass 2 and its fixed-point sums.
+struct PairI {
+  float4 pi, vi, di, li;
+  uint32_t idi, pri, seed;
+  int form;
+  float csx, csy, csz;
+  long long fx, fy, fz, px, py, pz;
+};
+
+// One pair term added to the particle's sums (the lane's share).
 template <bool PRESS>
+__device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, const PairTables& T,
+                                          PairI& I, int t, int dx, int dy, int dz) {
+  const float4 vj = __ldg(d.velf + t);
+  const uint32_t idj = fbits(vj.w);
+  if (idj == I.idi) return;  // nbdf_calculator.hpp:84
+  const float4 pj = __ldg(d.posf + t);
+  const float4 dj = __ldg(d.densf + t);
+  const float ex = (I.pi.x - (float)dx * I.csx) - pj.x;
+  const float ey = (I.pi.y - (float)dy * I.csy) - pj.y;
+  const float ez = (I.pi.z - (float)dz * I.csz) - pj.z;
+  const float dr2 = ex * ex + ey * ey + ez * ez;
+  const float inv_dr = rsqrtf(dr2);
+  const float dr = dr2 * inv_dr;
+  float w = 1.0f - dr;
+  if (dr2 > kNearCut2)  // admitted pairs have 1 - r >= 0 up to ~1e-13
+    w = fmaxf(near_cut_w(I.pi, I.li, pj, __ldg(d.poslo + t), dx, dy, dz, R, dr), 0.0f);
+  const float a = pair_all_cf(T, R, I.form, I.pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, I.vi, vj,
+                              I.di, dj, I.idi, idj, I.seed);
+  if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
+  const float gx = a * ex, gy = a * ey, gz = a * ez;
+  I.fx += fix_force(gx);
+  I.fy += fix_force(gy);
+  I.fz += fix_force(gz);
+  if (PRESS) {
+    I.px += fix_force(gx * ex);
+    I.py += fix_force(gy * ey);
+    I.pz += fix_force(gz * ez);
+  }
+}
+
+// One warp per particle. The list of pass 1 gives the pairs, 32 per round
+// with every lane busy; a particle whose list overflowed walks its cells
+// again and queues the in-range pairs in shared memory.
+template <int REACH, bool PRESS>
 __global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t qt[kWarps][64], qc[kWarps][64];
@@ -364,10 +461,13 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
   uint32_t* QC = qc[wid];
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
-  const uint32_t seed = R->seed + d.rep_time[r];
-  const int form = R->form;
-  const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
-  const int nseg = 2 * (2 * R->reach + 1) * (2 * R->reach + 1);
+  PairI I;
+  I.seed = R->seed + d.rep_time[r];
+  I.form = R->form;
+  I.csx = R->cs_f[0];
+  I.csy = R->cs_f[1];
+  I.csz = R->cs_f[2];
+  constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
   for (int s = s0; s < s_end; s++) {
@@ -380,102 +480,87 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
       __syncwarp();
       cached = cell;
     }
-    const float4 pi = d.posf[s];
-    const float4 vi = d.velf[s];
-    const float4 di = d.densf[s];
-    const float4 li = d.poslo[s];
-    const uint32_t idi = fbits(vi.w), pri = fbits(pi.w);
-    long long fx = 0, fy = 0, fz = 0, px = 0, py = 0, pz = 0;
-    int qn = 0;
-
-    // evaluates queue entries [0, cnt) with lane k on entry k
-    auto evaluate = [&](int cnt) {
-      if (lane < cnt) {
-        const int t = (int)QT[lane];
-        const PairCode pc = unpack_code(QC[lane]);
-        const float4 vj = __ldg(d.velf + t);
-        const uint32_t idj = fbits(vj.w);
-        if (idj != idi) {
-          const float4 pj = __ldg(d.posf + t);
-          const float4 dj = __ldg(d.densf + t);
-          const float ex = (pi.x - (float)pc.dx * csx) - pj.x;
-          const float ey = (pi.y - (float)pc.dy * csy) - pj.y;
-          const float ez = (pi.z - (float)pc.dz * csz) - pj.z;
-          const float dr2 = ex * ex + ey * ey + ez * ez;
-          const float inv_dr = rsqrtf(dr2);
-          const float dr = dr2 * inv_dr;
-          float w = 1.0f - dr;
-          if (dr2 > kNearCut2)  // admitted pairs have 1 - r >= 0 up to ~1e-13
-            w = fmaxf(near_cut_w(pi, li, pj, __ldg(d.poslo + t), pc.dx, pc.dy, pc.dz, R, dr), 0.0f);
-          const float a = pair_all_cf(T, R, form, pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, vi,
-                                      vj, di, dj, idi, idj, seed);
-          if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
-          const float gx = a * ex, gy = a * ey, gz = a * ez;
-          fx += fix_from_float(gx, kForceBits);
-          fy += fix_from_float(gy, kForceBits);
-          fz += fix_from_float(gz, kForceBits);
-          if (PRESS) {
-            px += fix_from_float(gx * ex, kForceBits);
-            py += fix_from_float(gy * ey, kForceBits);
-            pz += fix_from_float(gz * ez, kForceBits);
-          }
-        }
+    I.pi = d.posf[s];
+    I.vi = d.velf[s];
+    I.di = d.densf[s];
+    I.li = d.poslo[s];
+    I.idi = fbits(I.vi.w);
+    I.pri = fbits(I.pi.w);
+    I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
+    const uint32_t cnt = d.nbn[s];
+    if (cnt != kNbrFallback) {
+      const uint16_t* list = d.nbl + (size_t)s * kNbrCap;
+      for (int k = lane; k < (int)cnt; k += 32) {
+        const uint32_t e = list[k];
+        const int g = (int)(e & 63u);
+        const int code = S.code[g];
+        const int t = S.tb[g] + (int)(e >> 8);
+        eval_pair<PRESS>(d, R, T, I, t, (code & 7) - 4 + (int)((e >> 6) & 3u),
+                         ((code >> 3) & 7) - 4, ((code >> 6) & 7) - 4);
       }
-    };
-
-    for (int g = 0; g < nseg; g++) {
-      const int tb = S.tb[g], te = S.te[g];
-      if (tb >= te) continue;
-      const int code = S.code[g];
-      const int dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
-      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
-      for (int t0 = tb; t0 < te; t0 += 32) {
-        const int t = t0 + lane;
-        bool in = false;
-        int dx = 0;
-        if (t < te && t != s) {
-          const float4 pj = __ldg(d.posf + t);
-          dx = seg_dx(S, g, t);
-          const float ex = (pi.x - (float)dx * csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
-          const float dr2 = ex * ex + ey * ey + ez * ez;
-          if (dr2 < 1.0f + kGuard) {
-            in = dr2 < 1.0f;
-            if (fabsf(dr2 - 1.0f) <= kGuard) {
-              const PairCode pc = unpack_code(pack_code(dx, code));
-              in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
+    } else {
+      int qn = 0;
+#pragma unroll 1
+      for (int g = 0; g < nseg; g++) {
+        const int tb = S.tb[g], te = S.te[g];
+        if (tb >= te) continue;
+        const int code = S.code[g];
+        int b[2 * REACH];
+#pragma unroll
+        for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+        const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+        const float by = I.pi.y - (float)dy * I.csy, bz = I.pi.z - (float)dz * I.csz;
+        for (int t0 = tb; t0 < te; t0 += 32) {
+          const int t = t0 + lane;
+          bool in = false;
+          int dx = 0;
+          if (t < te && t != s) {
+            const float4 pj = __ldg(d.posf + t);
+            dx = fx0 + frame_step<REACH>(t, b);
+            const float ex = (I.pi.x - (float)dx * I.csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
+            const float dr2 = ex * ex + ey * ey + ez * ez;
+            if (dr2 < 1.0f + kGuard) {
+              in = dr2 < 1.0f;
+              if (fabsf(dr2 - 1.0f) <= kGuard) {
+                const PairCode pc = unpack_code(pack_code(dx, code));
+                in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
+              }
             }
           }
-        }
-        const uint32_t mask = __ballot_sync(0xffffffffu, in);
-        if (in) {
-          const int pos = qn + __popc(mask & lt_mask);
-          QT[pos] = (uint32_t)t;
-          QC[pos] = pack_code(dx, code);
-        }
-        qn += __popc(mask);
-        if (qn >= 32) {
-          __syncwarp();
-          evaluate(32);
-          __syncwarp();
-          if (lane < qn - 32) {
-            QT[lane] = QT[32 + lane];
-            QC[lane] = QC[32 + lane];
+          const uint32_t mask = __ballot_sync(0xffffffffu, in);
+          if (in) {
+            const int pos = qn + __popc(mask & lt_mask);
+            QT[pos] = (uint32_t)t;
+            QC[pos] = pack_code(dx, code);
           }
-          __syncwarp();
-          qn -= 32;
+          qn += __popc(mask);
+          if (qn >= 32) {
+            __syncwarp();
+            const PairCode pc = unpack_code(QC[lane]);
+            eval_pair<PRESS>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+            __syncwarp();
+            if (lane < qn - 32) {
+              QT[lane] = QT[32 + lane];
+              QC[lane] = QC[32 + lane];
+            }
+            __syncwarp();
+            qn -= 32;
+          }
         }
       }
+      __syncwarp();
+      if (lane < qn) {
+        const PairCode pc = unpack_code(QC[lane]);
+        eval_pair<PRESS>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+      }
+      __syncwarp();
     }
-    __syncwarp();
-    evaluate(qn);
-    __syncwarp();
-    fx = warp_sum_ll(fx);
-    fy = warp_sum_ll(fy);
-    fz = warp_sum_ll(fz);
+    const long long fx = warp_sum_ll(I.fx), fy = warp_sum_ll(I.fy), fz = warp_sum_ll(I.fz);
+    long long px = 0, py = 0, pz = 0;
     if (PRESS) {
-      px = warp_sum_ll(px);
-      py = warp_sum_ll(py);
-      pz = warp_sum_ll(pz);
+      px = warp_sum_ll(I.px);
+      py = warp_sum_ll(I.py);
+      pz = warp_sum_ll(I.pz);
     }
     if (lane == 0) {
       d.fqx[s] = fx;
@@ -570,7 +655,6 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
 
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st) {
-  (void)tu;
   if (nblk == 0) return;
   if (fp64) {
     if (with_press)
@@ -579,10 +663,17 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
       k_force_f64<false><<<nblk, kRowBlock, 0, st>>>(d);
     return;
   }
-  if (with_press)
-    k_force_f32<true><<<nblk, kRowBlock, 0, st>>>(d);
-  else
-    k_force_f32<false><<<nblk, kRowBlock, 0, st>>>(d);
+  if (tu.reach == 2) {
+    if (with_press)
+      k_force_f32<2, true><<<nblk, kRowBlock, 0, st>>>(d);
+    else
+      k_force_f32<2, false><<<nblk, kRowBlock, 0, st>>>(d);
+  } else {
+    if (with_press)
+      k_force_f32<1, true><<<nblk, kRowBlock, 0, st>>>(d);
+    else
+      k_force_f32<1, false><<<nblk, kRowBlock, 0, st>>>(d);
+  }
 }
 
 // -------------------------------------------- neighbour centre of mass

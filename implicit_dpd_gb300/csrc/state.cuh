@@ -38,9 +38,11 @@ struct DevState {
   uint32_t* scell;
   float4 *posf, *velf, *densf;
   float4* poslo;               // low-order parts of the cell-local position
-  long long *fqx, *fqy, *fqz;  // pair force, 2^-32 fixed point
+  uint16_t* nbl;               // [N * kNbrCap] in-range neighbours of pass 1 (sorted order)
+  uint16_t* nbn;               // [N] list length, or 0xffff when the list overflowed
+  long long *fqx, *fqy, *fqz;  // pair force, 2^-26 fixed point
   long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API only)
-  long long *dqx, *dqy, *dqz;  // partial densities, 2^-40 fixed point (fine-grained API only)
+  long long *dqx, *dqy, *dqz;  // partial densities in RepDev::dens_unscale units (fine-grained API only)
   double* dens64;              // [3N] partial densities of the plain FP64 arm (sorted order)
   // ---- topology
   uint32_t* topol;  // [4 * total molecules] storage rows
@@ -62,6 +64,7 @@ enum : int { kErrNone = 0, kErrCellOverflow = 1, kErrBadCell = 2, kErrListOverfl
              kErrNonFinite = 4, kErrComBox = 5 };
 
 constexpr int kRowBlock = 128;  // rows per block of row-block launches
+constexpr int kNbrCap = 256;    // neighbour-list slots per particle
 
 // kernels_cells.cu
 void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st);
@@ -76,7 +79,7 @@ void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
 struct PairTuning {
   int reach;       // 1: cells of the cutoff, 27-cell stencil; 2: half cells, 125-cell stencil
 };
-void launch_density(const DevState& d, int nblk, bool fp64, cudaStream_t st);
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);

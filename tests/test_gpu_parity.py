@@ -262,12 +262,15 @@ def test_cell_reach_gives_bit_identical_trajectories():
         assert np.array_equal(out[0][key], out[1][key]), key
 
 
-def test_dense_membrane_density_force_match_oracle():
-    """The compacted membrane regime (~150 neighbours per bead) exercises the
-    pair queue far beyond one warp's worth of neighbours."""
-    box = np.array([7.0, 7.0, 5.0])
+@pytest.mark.parametrize("rho", [30.0, 90.0])
+def test_dense_membrane_density_force_match_oracle(rho):
+    """The compacted membrane regime (~150 neighbours per bead at rho 30)
+    fills several 32-pair rounds per particle; at rho 90 the neighbour lists
+    overflow (> 256 entries, segments longer than 255 rows) and pass 2 walks
+    the cells again."""
+    box = np.array([7.0, 7.0, 5.0]) if rho < 50 else np.array([5.0, 5.0, 5.0])
     rng = np.random.default_rng(12)
-    st = configs.liquid(box, 30.0, seed=12, prop=1)
+    st = configs.liquid(box, rho, seed=12, prop=1)
     st["prop"] = rng.integers(0, 3, len(st["pos"])).astype(np.uint32)
     p = mdpd_params(box, time=3)
     dens, cm, cnt, acc, press = oracle_forces(p, st)
