@@ -117,21 +117,58 @@ struct Saru {
 // -ln u1 is taken from the exact complement 1 - u1 through log1p when u1 >=
 // 1/2, and the cosine argument is folded to (0, 1) in integers, so neither
 // factor loses relative accuracy at the ends of the interval.
+//
+// Both factors are evaluated without branches (lanes of a warp take
+// different ends of the interval):
+//  * u1 < 1/2: -ln u1 = -log2(u1) ln 2 with the hardware log2, whose error is
+//    below 2 ulp of |log2 u1| >= 1;
+//  * u1 >= 1/2: c = 1 - u1 comes exactly from the integer complement and
+//    -ln(1 - c) = 2 atanh(z), z = c / (2 - c) <= 1/3, from its Taylor series
+//    z + z^3/3 + ... + z^15/15 (truncation below 1e-8 relative);
+//  * cos(pi x): x is folded in integers to y in [0, 1/2] with a sign, then
+//    cos(pi y) for y <= 1/4 or sin(pi (1/2 - y)) from Taylor polynomials of
+//    degree 10 / 9 in pi y <= pi/4 (truncation below 2e-9).
 __device__ __forceinline__ float saru_nrml_f32(Saru& s) {
-  const uint32_t d1 = s.next();
-  const uint32_t d2 = s.next();
-  const uint32_t m1 = d1 | 1u;  // 2 (d1 >> 1) + 1
-  float nlog;
-  if (m1 < 0x80000000u) {
-    nlog = -logf(__uint2float_rn(m1) * 2.3283064365386963e-10f);  // 2^-32
-  } else {
-    const uint32_t c = 0u - m1;  // 2^32 - m1: exact complement, odd
-    nlog = -log1pf(-(__uint2float_rn(c) * 2.3283064365386963e-10f));
-  }
-  uint32_t m2 = d2 | 1u;
-  if (m2 > 0x80000000u) m2 = 0u - m2;  // cos(pi x) = cos(pi (2 - x))
-  const float cs = cospif(__uint2float_rn(m2) * 4.6566128730773926e-10f);  // 2^-31
-  return sqrtf(2.0f * nlog) * cs;
+  const uint32_t m1 = s.next() | 1u;  // 2 (draw >> 1) + 1 = u1 * 2^32
+  const uint32_t m2 = s.next() | 1u;  // u2 * 2^32
+  const float two_m32 = 2.3283064365386963e-10f;  // 2^-32
+  const float la = -__log2f(__uint2float_rn(m1) * two_m32) * 0.69314718055994531f;
+  const float c = __uint2float_rn(0u - m1) * two_m32;  // 1 - u1, exact complement
+  const float z = __fdividef(c, 2.0f - c);
+  const float z2 = z * z;
+  float p = 1.0f / 15.0f;
+  p = fmaf(p, z2, 1.0f / 13.0f);
+  p = fmaf(p, z2, 1.0f / 11.0f);
+  p = fmaf(p, z2, 1.0f / 9.0f);
+  p = fmaf(p, z2, 1.0f / 7.0f);
+  p = fmaf(p, z2, 1.0f / 5.0f);
+  p = fmaf(p, z2, 1.0f / 3.0f);
+  p = fmaf(p, z2, 1.0f);
+  const float lb = 2.0f * z * p;
+  const float nlog = m1 < 0x80000000u ? la : lb;
+  // cos(2 pi u2) = cos(pi x), x = m2 / 2^31 in (0, 2)
+  uint32_t n = m2 > 0x80000000u ? 0u - m2 : m2;         // x -> 2 - x: x in (0, 1]
+  const float sgn = n > 0x40000000u ? -1.0f : 1.0f;     // cos(pi x) = -cos(pi (1 - x))
+  n = n > 0x40000000u ? 0x80000000u - n : n;            // y = n / 2^31 in [0, 1/2]
+  const bool use_cos = n <= 0x20000000u;                // y <= 1/4
+  const uint32_t a = use_cos ? n : 0x40000000u - n;     // pi y or pi (1/2 - y), <= pi/4
+  const float t = __uint2float_rn(a) * (3.14159265358979323846f * 4.6566128730773926e-10f);
+  const float t2 = t * t;
+  float pc = -1.0f / 3628800.0f;
+  pc = fmaf(pc, t2, 1.0f / 40320.0f);
+  pc = fmaf(pc, t2, -1.0f / 720.0f);
+  pc = fmaf(pc, t2, 1.0f / 24.0f);
+  pc = fmaf(pc, t2, -0.5f);
+  pc = fmaf(pc, t2, 1.0f);
+  float ps = 1.0f / 362880.0f;
+  ps = fmaf(ps, t2, -1.0f / 5040.0f);
+  ps = fmaf(ps, t2, 1.0f / 120.0f);
+  ps = fmaf(ps, t2, -1.0f / 6.0f);
+  ps = fmaf(ps, t2, 1.0f);
+  ps = ps * t;
+  const float cs = sgn * (use_cos ? pc : ps);
+  const float r2 = 2.0f * nlog;
+  return r2 * rsqrtf(r2) * cs;  // nlog > 0 for every odd m1
 }
 
 // FP64 normal exactly as the reference computes it (plain FP64 arm).

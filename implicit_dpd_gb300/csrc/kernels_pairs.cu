@@ -143,16 +143,31 @@ __device__ __forceinline__ int frame_step(int t, const int* b) {
   return k;
 }
 
-// One warp per particle: partial densities (FP32 pair weights summed as
-// fixed-point integers, see the file comment) and the list of neighbours
-// within the pair cutoff that pass 2 evaluates.
+// Density weight of one in-range pair (pass 1 arithmetic, FP32) in the
+// 2^-23 fixed point of the replica: round(w * pre * 2^23) read from the
+// mantissa of 1 + w * pre (w * pre in [0, 1]).
+__device__ __forceinline__ uint32_t dens_weight(float dr2, bool warren, float inv_rd, float wnorm,
+                                                float pre) {
+  const float dr = dr2 * rsqrtf(dr2);
+  float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
+  w = warren ? wnorm * (w * w) : w * w;
+  return (uint32_t)(__float_as_int(fmaf(w, pre, 1.0f)) - 0x3f800000);
+}
+
+// One warp per particle. Phase A sweeps the neighbour segments 32
+// candidates at a time and appends the pairs within the cutoff 1 to a list
+// in shared memory; phase B takes the density weights from that list with
+// every lane busy and copies the list out for pass 2. A particle whose list
+// overflows takes its weights during a second sweep instead.
 template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
+  __shared__ uint32_t lst32[kWarps][kNbrCap / 2];
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
+  uint16_t* L = reinterpret_cast<uint16_t*>(lst32[wid]);
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
@@ -174,10 +189,10 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       cached = cell;
     }
     const float4 pi = d.posf[s];
-    uint16_t* list = d.nbl + (size_t)s * kNbrCap;
-    uint32_t q0 = 0, q1 = 0, q2 = 0;
+    const uint32_t si = d.perm[s];
     int nl = 0;
     bool lost = false;
+    // ---- phase A: the pairs within the cutoff 1
 #pragma unroll 1
     for (int g = 0; g < nseg; g++) {
       const int tb = S.tb[g], te = S.te[g];
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
       for (int t0 = tb; t0 < te; t0 += 32) {
         const int t = t0 + lane;
-        bool in1 = false;  // within the pair cutoff 1
+        bool in1 = false;
         int ddx = 0;
         if (t < te && t != s) {
           const float4 pj = __ldg(d.posf + t);
@@ -198,40 +213,81 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
           const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
                       ez = bz - pj.z;
           const float dr2 = ex * ex + ey * ey + ez * ez;
-          if (dr2 < 1.0f + kGuard) {
-            in1 = dr2 < 1.0f;
-            bool ind = dr2 < cutd2 && dr2 >= 1.0e-10f;  // density weight taken
-            const bool near1 = fabsf(dr2 - 1.0f) <= kGuard;
-            const bool neard = warren ? fabsf(dr2 - cutd2) <= kGuard : near1;
-            if (near1 || neard || dr2 < 1.0e-10f) {
-              const PairCode pc = unpack_code(pack_code(fx0 + ddx, code));
-              const double e2 = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz);
-              in1 = e2 < 1.0;
-              ind = e2 < cutd2d && e2 != 0.0;
-            }
-            if (ind) {
-              const float dr = sqrtf(dr2);
-              float w = warren ? 1.0f - dr * inv_rd : 1.0f - dr;
-              w = warren ? wnorm * (w * w) : w * w;
-              // round(w * pre * 2^23) from the mantissa of 1 + w * pre, w * pre in [0, 1]
-              const uint32_t v = (uint32_t)(__float_as_int(fmaf(w, pre, 1.0f)) - 0x3f800000);
-              const uint32_t pr = fbits(pj.w);
-              q0 += pr == 0 ? v : 0u;
-              q1 += pr == 1 ? v : 0u;
-              q2 += pr == 2 ? v : 0u;
-            }
+          in1 = dr2 < 1.0f;
+          if (fabsf(dr2 - 1.0f) <= kGuard) {
+            const PairCode pc = unpack_code(pack_code(fx0 + ddx, code));
+            in1 = exact_dr2(d, R, si, d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
           }
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, in1);
         const int off = t - tb;
         if (in1) {
           const int pos = nl + __popc(mask & lt_mask);
-          if (pos < kNbrCap) list[pos] = nbr_entry(g, ddx, off);
+          if (pos < kNbrCap) L[pos] = nbr_entry(g, ddx, off);
         }
         lost |= __any_sync(0xffffffffu, in1 && off > 255);
         nl += __popc(mask);
       }
     }
+    __syncwarp();
+    // ---- phase B: density weights
+    uint32_t q0 = 0, q1 = 0, q2 = 0;
+    const bool fits = nl <= kNbrCap && !lost;
+    auto take = [&](int t, int dx, int dy, int dz, float4 pj) {
+      const float ex = (pi.x - (float)dx * csx) - pj.x;
+      const float ey = (pi.y - (float)dy * csy) - pj.y;
+      const float ez = (pi.z - (float)dz * csz) - pj.z;
+      const float dr2 = ex * ex + ey * ey + ez * ez;
+      bool ind = dr2 < cutd2 && dr2 >= 1.0e-10f;
+      if ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f) {
+        // image shifts of the pair follow from the frame offsets and the cells
+        int cxi, cyi, czi, cxj, cyj, czj;
+        cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cxi, cyi, czi);
+        cell_xyz((int)d.scell[t] - R->cell_off, R->nc, cxj, cyj, czj);
+        const int rs = R->rshift;
+        const int sx = ((cxi >> rs) + dx - (cxj >> rs)) / R->nf[0];
+        const int sy = ((cyi >> rs) + dy - (cyj >> rs)) / R->nf[1];
+        const int sz = ((czi >> rs) + dz - (czj >> rs)) / R->nf[2];
+        const double e2 = exact_dr2(d, R, si, d.perm[t], sx, sy, sz);
+        ind = e2 < cutd2d && e2 != 0.0;
+      }
+      if (ind) {
+        const uint32_t v = dens_weight(dr2, warren, inv_rd, wnorm, pre);
+        const uint32_t pr = fbits(pj.w);
+        q0 += pr == 0 ? v : 0u;
+        q1 += pr == 1 ? v : 0u;
+        q2 += pr == 2 ? v : 0u;
+      }
+    };
+    if (fits) {
+      for (int k = lane; k < nl; k += 32) {
+        const uint32_t e = L[k];
+        const int g = (int)(e & 63u);
+        const int code = S.code[g];
+        const int t = S.tb[g] + (int)(e >> 8);
+        take(t, (code & 7) - 4 + (int)((e >> 6) & 3u), ((code >> 3) & 7) - 4,
+             ((code >> 6) & 7) - 4, __ldg(d.posf + t));
+      }
+      // list out for pass 2: 4-byte words, coalesced
+      uint32_t* out = reinterpret_cast<uint32_t*>(d.nbl + (size_t)s * kNbrCap);
+      for (int k = lane; k < (nl + 1) / 2; k += 32) out[k] = lst32[wid][k];
+    } else {
+#pragma unroll 1
+      for (int g = 0; g < nseg; g++) {
+        const int tb = S.tb[g], te = S.te[g];
+        if (tb >= te) continue;
+        const int code = S.code[g];
+        int b[2 * REACH];
+#pragma unroll
+        for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+        const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+        for (int t0 = tb; t0 < te; t0 += 32) {
+          const int t = t0 + lane;
+          if (t < te && t != s) take(t, fx0 + frame_step<REACH>(t, b), dy, dz, __ldg(d.posf + t));
+        }
+      }
+    }
+    __syncwarp();
     unsigned long long a0 = q0, a1 = q1, a2 = q2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -243,7 +299,7 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       const float u = R->dens_unscale_f;
       d.densf[s] = make_float4(fix_to_float((long long)a0, u), fix_to_float((long long)a1, u),
                                fix_to_float((long long)a2, u), 0.0f);
-      d.nbn[s] = (nl > kNbrCap || lost) ? (uint16_t)kNbrFallback : (uint16_t)nl;
+      d.nbn[s] = fits ? (uint16_t)nl : (uint16_t)kNbrFallback;
       if (d.dqx) {
         d.dqx[s] = (long long)a0;
         d.dqy[s] = (long long)a1;
@@ -344,7 +400,7 @@ __device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* 
                                              float w, float ex, float ey, float ez, float4 vi,
                                              float4 vj, float4 di, float4 dj, uint32_t idi,
                                              uint32_t idj, uint32_t seed) {
-  const float sqw = sqrtf(w);
+  const float sqw = w > 0.0f ? w * rsqrtf(w) : 0.0f;  // sqrt(1 - r), 2 ulp
   const int k = pri * 3 + prj;
   float cons;
   if (form == IDPD_FORM_PAIRWISE_K) {
@@ -440,7 +496,7 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
 // with every lane busy; a particle whose list overflowed walks its cells
 // again and queues the in-range pairs in shared memory.
 template <int REACH, bool PRESS>
-__global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
+__global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t qt[kWarps][64], qc[kWarps][64];
   __shared__ PairTables T;
@@ -490,8 +546,10 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f32(DevState d) {
     const uint32_t cnt = d.nbn[s];
     if (cnt != kNbrFallback) {
       const uint16_t* list = d.nbl + (size_t)s * kNbrCap;
+      uint32_t e_next = lane < (int)cnt ? list[lane] : 0u;  // one round ahead
       for (int k = lane; k < (int)cnt; k += 32) {
-        const uint32_t e = list[k];
+        const uint32_t e = e_next;
+        if (k + 32 < (int)cnt) e_next = list[k + 32];
         const int g = (int)(e & 63u);
         const int code = S.code[g];
         const int t = S.tb[g] + (int)(e >> 8);
