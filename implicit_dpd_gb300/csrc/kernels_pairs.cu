@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
       for (int t0 = tb; t0 < te; t0 += 32) {
         const int t = t0 + lane;
-        bool in1 = false;
+        bool in1 = false, near = false;
         int ddx = 0;
         if (t < te && t != s) {
           const float4 pj = __ldg(d.posf + t);
@@ -214,7 +214,12 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
                       ez = bz - pj.z;
           const float dr2 = ex * ex + ey * ey + ez * ez;
           in1 = dr2 < 1.0f;
-          if (fabsf(dr2 - 1.0f) <= kGuard) {
+          near = fabsf(dr2 - 1.0f) <= kGuard;
+        }
+        // rare: a warp-uniform branch keeps the FP64 recheck out of the
+        // common path (a plain branch would be if-converted)
+        if (__any_sync(0xffffffffu, near)) {
+          if (near) {
             const PairCode pc = unpack_code(pack_code(fx0 + ddx, code));
             in1 = exact_dr2(d, R, si, d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
           }
@@ -233,13 +238,16 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
     // ---- phase B: density weights
     uint32_t q0 = 0, q1 = 0, q2 = 0;
     const bool fits = nl <= kNbrCap && !lost;
-    auto take = [&](int t, int dx, int dy, int dz, float4 pj) {
+    // weight of one pair; called by every lane together (valid = false for
+    // lanes without a pair) so that the rare FP64 recheck is warp-uniform
+    auto take = [&](bool valid, int t, int dx, int dy, int dz, float4 pj) {
       const float ex = (pi.x - (float)dx * csx) - pj.x;
       const float ey = (pi.y - (float)dy * csy) - pj.y;
       const float ez = (pi.z - (float)dz * csz) - pj.z;
       const float dr2 = ex * ex + ey * ey + ez * ez;
-      bool ind = dr2 < cutd2 && dr2 >= 1.0e-10f;
-      if ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f) {
+      bool ind = valid && dr2 < cutd2 && dr2 >= 1.0e-10f;
+      const bool recheck = valid && ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f);
+      if (__any_sync(0xffffffffu, recheck) && recheck) {
         // image shifts of the pair follow from the frame offsets and the cells
         int cxi, cyi, czi, cxj, cyj, czj;
         cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cxi, cyi, czi);
@@ -260,13 +268,15 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       }
     };
     if (fits) {
-      for (int k = lane; k < nl; k += 32) {
-        const uint32_t e = L[k];
+      for (int k0 = 0; k0 < nl; k0 += 32) {
+        const int k = k0 + lane;
+        const bool valid = k < nl;
+        const uint32_t e = valid ? L[k] : 0u;
         const int g = (int)(e & 63u);
         const int code = S.code[g];
         const int t = S.tb[g] + (int)(e >> 8);
-        take(t, (code & 7) - 4 + (int)((e >> 6) & 3u), ((code >> 3) & 7) - 4,
-             ((code >> 6) & 7) - 4, __ldg(d.posf + t));
+        take(valid, t, (code & 7) - 4 + (int)((e >> 6) & 3u), ((code >> 3) & 7) - 4,
+             ((code >> 6) & 7) - 4, valid ? __ldg(d.posf + t) : pi);
       }
       // list out for pass 2: 4-byte words, coalesced
       uint32_t* out = reinterpret_cast<uint32_t*>(d.nbl + (size_t)s * kNbrCap);
@@ -283,7 +293,8 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
         const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
         for (int t0 = tb; t0 < te; t0 += 32) {
           const int t = t0 + lane;
-          if (t < te && t != s) take(t, fx0 + frame_step<REACH>(t, b), dy, dz, __ldg(d.posf + t));
+          const bool valid = t < te && t != s;
+          take(valid, t, fx0 + frame_step<REACH>(t, b), dy, dz, valid ? __ldg(d.posf + t) : pi);
         }
       }
     }
@@ -572,18 +583,18 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
           const int t = t0 + lane;
           bool in = false;
           int dx = 0;
+          bool near = false;
           if (t < te && t != s) {
             const float4 pj = __ldg(d.posf + t);
             dx = fx0 + frame_step<REACH>(t, b);
             const float ex = (I.pi.x - (float)dx * I.csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
             const float dr2 = ex * ex + ey * ey + ez * ez;
-            if (dr2 < 1.0f + kGuard) {
-              in = dr2 < 1.0f;
-              if (fabsf(dr2 - 1.0f) <= kGuard) {
-                const PairCode pc = unpack_code(pack_code(dx, code));
-                in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
-              }
-            }
+            in = dr2 < 1.0f;
+            near = fabsf(dr2 - 1.0f) <= kGuard;
+          }
+          if (__any_sync(0xffffffffu, near) && near) {
+            const PairCode pc = unpack_code(pack_code(dx, code));
+            in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
           }
           const uint32_t mask = __ballot_sync(0xffffffffu, in);
           if (in) {
