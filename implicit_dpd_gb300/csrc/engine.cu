@@ -30,6 +30,10 @@ struct Staged {  // one replica's rows as uploaded (upload order)
 
 }  // namespace
 
+namespace idpd {
+void set_library_error(const char* msg) { g_lib_err = msg; }
+}  // namespace idpd
+
 struct idpd_handle {
   int device = 0;
   int flags = 0;

@@ -207,6 +207,52 @@ __global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
                           __double2float_rn(d.vz[i]), __uint_as_float(d.id[i]));
 }
 
+void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cudaStream_t st) {
+  const int nb = (ncell + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell);
+  k_scan_parts<<<1, kScanThreads, 0, st>>>(part, nb);
+  k_scan_finish<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, n_tot);
+}
+
+void launch_cell_sort_raw(uint32_t* perm, const int* start, int ncell, cudaStream_t st) {
+  if (ncell > 0) k_cell_sort<<<(ncell + 255) / 256, 256, 0, st>>>(perm, start, ncell);
+}
+
+// Cell index and arrival slot of rows given as x y z triples (one grid, no
+// replicas): the binning of k_drift_bin without the drift.
+__global__ void __launch_bounds__(256) k_bin_rows(const double* pos, int n, double ix, double iy,
+                                                  double iz, int nx, int ny, int nz,
+                                                  uint32_t* cell, uint32_t* slot, int* cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* p = pos + 3 * (size_t)i;
+  const int cx = cell_coord(p[0], ix, nx);
+  const int cy = cell_coord(p[1], iy, ny);
+  const int cz = cell_coord(p[2], iz, nz);
+  const uint32_t c = (uint32_t)((cz * ny + cy) * nx + cx);
+  cell[i] = c;
+  slot[i] = (uint32_t)atomicAdd(&cnt[c], 1);
+}
+
+__global__ void __launch_bounds__(256) k_scatter_rows(const uint32_t* cell, const uint32_t* slot,
+                                                      const int* start, int n, uint32_t* perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  perm[(uint32_t)start[cell[i]] + slot[i]] = (uint32_t)i;
+}
+
+void launch_bin_rows(const double* pos, int n, const double inv_cs[3], const int nc[3],
+                     uint32_t* cell, uint32_t* slot, int* cnt, cudaStream_t st) {
+  if (n > 0)
+    k_bin_rows<<<(n + 255) / 256, 256, 0, st>>>(pos, n, inv_cs[0], inv_cs[1], inv_cs[2], nc[0],
+                                                nc[1], nc[2], cell, slot, cnt);
+}
+
+void launch_scatter_rows(const uint32_t* cell, const uint32_t* slot, const int* start, int n,
+                         uint32_t* perm, cudaStream_t st) {
+  if (n > 0) k_scatter_rows<<<(n + 255) / 256, 256, 0, st>>>(cell, slot, start, n, perm);
+}
+
 void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st) {
   if (nblk == 0) return;
   k_drift_bin<<<nblk, kRowBlock, 0, st>>>(d, do_drift ? 1 : 0);

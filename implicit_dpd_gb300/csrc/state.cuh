@@ -74,6 +74,20 @@ void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool s
 void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol,
                     cudaStream_t st);
 void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
+// Counting-sort pieces on raw arrays: exclusive scan of cnt into start
+// (start[ncell] = n_tot, cnt cleared; part holds ncell / 4096 + 1 ints) and
+// the per-cell ascending order of perm.
+void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cudaStream_t st);
+void launch_cell_sort_raw(uint32_t* perm, const int* start, int ncell, cudaStream_t st);
+// Binning of n rows (x y z triples) on one grid of nc cells per axis, and the
+// scatter of rows to their sorted slots.
+void launch_bin_rows(const double* pos, int n, const double inv_cs[3], const int nc[3],
+                     uint32_t* cell, uint32_t* slot, int* cnt, cudaStream_t st);
+void launch_scatter_rows(const uint32_t* cell, const uint32_t* slot, const int* start, int n,
+                         uint32_t* perm, cudaStream_t st);
+
+// engine.cu: sets the message that idpd_last_error returns for a NULL handle.
+void set_library_error(const char* msg);
 
 // kernels_pairs.cu
 struct PairTuning {

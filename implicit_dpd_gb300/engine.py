@@ -28,6 +28,7 @@ EXPORTS = [
     "idpd_bonded", "idpd_kick", "idpd_remove_cmdrift", "idpd_step", "idpd_sync",
     "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
     "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
+    "idpd_cell_order_noalloc",
 ]
 
 _lib = None
@@ -69,6 +70,7 @@ def load(path=LIB_PATH):
     L.idpd_set_dynamics.argtypes = [H, C.c_int32, VP, VP, VP]
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
+    L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
     _lib = L
     return L
 

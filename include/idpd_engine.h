@@ -210,6 +210,39 @@ int idpd_saru_nrml_f32(int32_t n, const uint32_t* s1, const uint32_t* s2, const 
  * pair cutoff 1.0). perm[k] = row at sorted position k. */
 int idpd_cell_order(idpd_handle* h, int32_t replica, uint32_t* cell_of_row, uint32_t* perm);
 
+/* ---- cell order without allocation ---------------------------------------
+ * No counterpart in the reference. The same cell index per row and stable
+ * cell-sorted order as idpd_cell_order, for rows the caller already holds on
+ * the device, computed without allocating any device memory. It is meant for
+ * callers that cannot call cudaMalloc: a host MD code whose own memory pool
+ * owns the device budget, or a step loop that must not pay the device-wide
+ * synchronisation that cudaMalloc / cudaFree can cause.
+ *
+ * Its scratch is one static device array of IDPD_NOALLOC_SCRATCH_BYTES
+ * (about 8 MiB), which every GPU that loads this library holds until the
+ * process exits. Limits: n <= IDPD_NOALLOC_MAX_ROWS and
+ * floor(box[0]) * floor(box[1]) * floor(box[2]) <= IDPD_NOALLOC_MAX_CELLS;
+ * larger inputs return IDPD_ERR_CAPACITY with a message.
+ *
+ *   pos          device, n rows of x y z (FP64) inside [0, box)
+ *   box          host, the three box sides, each >= 1.0
+ *   cell_of_row  device out, n cell indices ((cz ny + cy) nx + cx)
+ *   perm         device out, perm[k] = row at sorted position k
+ *   stream       cudaStream_t to queue the work on (NULL: default stream)
+ *
+ * The call queues its work and returns; the outputs are complete when the
+ * stream reaches that point. The first call on each device, made with that
+ * device current, looks up the scratch address once: make that first call
+ * before any stream capture. All calls share the one array, which keeps the
+ * last call's contents, so calls that overlap on the GPU (other streams,
+ * other threads) race and corrupt each other's results: serialise them.
+ * Errors are read with idpd_last_error(NULL, ...). */
+#define IDPD_NOALLOC_MAX_ROWS (1 << 20)
+#define IDPD_NOALLOC_MAX_CELLS (1 << 19)
+#define IDPD_NOALLOC_SCRATCH_BYTES 8389888
+int idpd_cell_order_noalloc(const double* pos, int32_t n, const double* box,
+                            uint32_t* cell_of_row, uint32_t* perm, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
