@@ -39,9 +39,15 @@ BOX = np.array([64.0, 64.0, 48.0])
 N_LAYERS = 10
 AREA_PER_LIPID = 0.333
 METRIC = "particle-steps/s on 1 GB300: FP32+batched vs plain FP64 kernel at stated force err"
-# force kernel algorithmic HBM bytes per particle: posf, velf, densf of the
-# particle itself (3 x 16 B) and its fixed-point force (3 x 8 B)
-FORCE_BYTES_PER_PARTICLE = 72
+# Algorithmic HBM bytes per particle of the two pair passes: the density pass
+# reads the particle's posf (16 B) and writes its densf (16 B); the force pass
+# reads posf, velf, densf (3 x 16 B) and writes the fixed-point force (3 x 8 B).
+PAIR_KERNELS = {
+    "density": {"kernel": "k_density_f32", "bytes_per_particle": 32,
+                "profile": "density_membrane_1m.md"},
+    "force": {"kernel": "k_force_f32", "bytes_per_particle": 72,
+              "profile": "force_membrane_1m.md"},
+}
 STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
 KERNELS_PER_STEP = 14          # drift_bin, scan x3, scatter, cell_sort, pack,
                                # density, force, bonded_kick, cmdrift x3, time
@@ -60,16 +66,25 @@ def workload(box=BOX, layers=N_LAYERS, seed=20250101):
     return st, n_amp, rp
 
 
-def workload_desc(n, n_amp):
+def workload_name(box=BOX, layers=N_LAYERS):
+    box = np.asarray(box, np.float64)
+    if np.array_equal(box, BOX) and layers == N_LAYERS:
+        return "membrane_1m"
+    return "membrane_{:g}x{:g}x{:g}_{}layers".format(*box, layers)
+
+
+def workload_desc(n, n_amp, box=BOX, layers=N_LAYERS):
     return {
-        "workload": "membrane_1m",
-        "description": ("10 flat bilayers of 1H+3T chains stacked in a periodic 64x64x48 box, "
+        "workload": workload_name(box, layers),
+        "description": (f"{layers} flat bilayers of 1H+3T chains stacked in a periodic "
+                        "{:g}x{:g}x{:g} box, ".format(*box) +
                         "reference MDPD form (chi 30, kappa 100, rho_co 40, vbb 0.1), sigma 3, "
                         "dt 0.005, cf_s 50, cf_b 10; timed after the equilibration steps, when "
-                        "the bilayers have compacted to ~150 in-range neighbours per bead"),
+                        "the bilayers have compacted to ~130 in-range neighbours per bead"),
         "n_particles": int(n),
         "n_molecules": int(n_amp),
-        "l2": "inputs larger than L2 (device state ~200 MB per replica)",
+        "l2": ("inputs larger than L2: the pair passes read posf, poslo, velf, densf and the "
+               f"neighbour list, ~{n * 344 / 1e6:.0f} MB per step against a 129 MB L2"),
     }
 
 
@@ -163,9 +178,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per force-kernel launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "force_membrane_1m.md")
+def profiled_traffic(name):
+    """DRAM bytes per launch of a kernel from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -177,11 +192,10 @@ def profiled_traffic():
     return None
 
 
-def equilibrated_slab(threads, equil=2000):
-    """A bounded CPU sample of the equilibrated workload: one bilayer of an
-    8 x 8 x 4.8 periodic slab taken through `equil` oracle steps (the same
-    compaction the timed GPU state went through), tiled 8 x 8 into one
-    bilayer period of membrane_1m (64 x 64 x 4.8, 98,304 beads)."""
+def equilibrated_patch(threads, equil=2000):
+    """One bilayer of an 8 x 8 x 4.8 periodic patch of membrane_1m taken
+    through `equil` oracle steps (the compaction the timed GPU state went
+    through). Returns (state, patch box, molecules, params)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
 
@@ -194,15 +208,33 @@ def equilibrated_slab(threads, equil=2000):
     for _ in range(equil):
         O.md_step(p, st, nthreads=threads)
     st["pos"] -= np.floor(st["pos"] / small) * small
+    return st, small, n_amp, p
+
+
+def tile_patch(patch, reps):
+    """reps = (nx, ny) periodic copies of the equilibrated patch side by side:
+    a bilayer of membrane_1m of (8 nx) x (8 ny) x 4.8."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+
+    st, small, n_amp, p = patch
     big, box = configs.tile({k: st[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")},
-                            small, (8, 8, 1))
-    n_amp_big = n_amp * 64
+                            small, (reps[0], reps[1], 1))
+    n_amp_big = n_amp * reps[0] * reps[1]
     rp_big = configs.run_param(box, dt=0.005, cf_r=3.0, cf_s=50.0, cf_b=10.0, vbb=0.1, chi=30.0,
                                kappa=100.0, rho_co=40.0)
     pb = O.derive_params(rp_big)
     pb.seed, pb.time = 1, p.time
     big["topol"], big["cf_bend"] = O.build_topology(big["amp_id"], big["unit"], n_amp_big, [],
                                                     pb.cf_b, pb.cf_b_rigid)
+    return big, n_amp_big, pb, box
+
+
+def equilibrated_slab(threads, equil=2000):
+    """A bounded CPU sample of the equilibrated workload: the equilibrated
+    patch tiled 8 x 8 into one bilayer period of membrane_1m (64 x 64 x 4.8,
+    98,304 beads)."""
+    big, n_amp_big, pb, _ = tile_patch(equilibrated_patch(threads, equil), (8, 8))
     return big, n_amp_big, pb
 
 
@@ -231,14 +263,27 @@ def cpu_baseline(min_seconds=10.0, max_steps=50):
                       f"bead), FP64 C oracle, OpenMP"}
 
 
-def run_reference(args, rank, world):
+def run_reference(args, rank, world, budget_s=90.0):
+    """The reference's CPU algorithm (the C oracle, every host thread) on a
+    sample of the equilibrated membrane sized so that warm-up plus timed steps
+    take about `budget_s` seconds."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
 
     threads = os.cpu_count() or 1
-    st, n_amp, p = equilibrated_slab(threads)
+    patch = equilibrated_patch(threads)
+    # rate of the oracle on one bilayer period, then the sample that fits the budget
+    probe, _, pp, _ = tile_patch(patch, (8, 8))
+    t0 = time.perf_counter()
+    O.md_step(pp, probe, nthreads=threads)
+    rate = len(probe["pos"]) / (time.perf_counter() - t0)
+    per_step = budget_s / max(1, args.steps + args.warmup)
+    tiles = int(min(64, max(1, rate * per_step // len(patch[0]["pos"]))))
+    ny = min(8, tiles)
+    nx = max(1, tiles // ny)
+    st, n_amp, p, box = tile_patch(patch, (nx, ny))
     for _ in range(args.warmup):
         O.md_step(p, st, nthreads=threads)
     t0 = time.perf_counter()
@@ -247,10 +292,10 @@ def run_reference(args, rank, world):
     dt = time.perf_counter() - t0
     n = len(st["pos"])
     value = n * args.steps / dt
-    sample = (f"each step one MD step (drift, density, force, bonded, kick) of one equilibrated "
-              f"bilayer period of membrane_1m (64x64x4.8, {n} beads, ~150 neighbours per bead), "
-              f"FP64 C oracle of the reference algorithm, OpenMP")
-    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": 0,
+    sample = (f"each step one MD step (drift, density, force, bonded, kick) of an equilibrated "
+              f"bilayer patch of membrane_1m ({box[0]:g}x{box[1]:g}x{box[2]:g}, {n} beads, "
+              f"~150 neighbours per bead), FP64 C oracle of the reference algorithm, OpenMP")
+    out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "config": workload_desc(n, n_amp), "impl": "reference",
@@ -261,12 +306,34 @@ def run_reference(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
-def make_engine(st, n_amp, rp, flags=0):
+def save_state(path, e, n_amp, box, layers, reach):
+    out = e.download()
+    np.savez(path, box=box, layers=layers, n_amp=n_amp, reach=reach, time=e.get_params().time,
+             **{k: out[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")})
+
+
+def run_kernel_case(path, device=0):
+    """Three graph-launched steps from a saved equilibrated state: few
+    launches before the pair passes, for kernel profiles of one launch."""
+    z = np.load(path)
+    box, layers = z["box"], int(z["layers"])
+    st = {k: z[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")}
+    rp = workload(box=box, layers=layers)[2]
+    e = make_engine(st, int(z["n_amp"]), rp, device=device)
+    e.set_tuning(int(z["reach"]))
+    e.step(3)
+    e.sync()
+    print(json.dumps({"kernel_case": workload_name(box, layers), "n_particles": len(st["pos"]),
+                      "steps": 3, "reach": int(z["reach"])}), flush=True)
+    e.close()
+
+
+def make_engine(st, n_amp, rp, flags=0, device=0):
     from implicit_dpd_gb300.engine import Engine, derive_params
 
     p = derive_params(rp)
     p.seed, p.time = 12345, 1
-    e = Engine(flags=flags, sort_period=100)
+    e = Engine(flags=flags, sort_period=100, device=device)
     e.set_params(p)
     e.upload(st)
     e.build_topology(n_amp)
@@ -298,15 +365,18 @@ def run_engine(args, rank, world, local_rank):
     from implicit_dpd_gb300.abi import CFG_FP64_PAIRS
 
     dist = Dist(world)
-    st, n_amp, rp = workload()
+    box, layers = np.asarray(args.box, np.float64), args.layers
+    st, n_amp, rp = workload(box=box, layers=layers)
     n = len(st["pos"])
-    e = make_engine(st, n_amp, rp)
+    e = make_engine(st, n_amp, rp, device=local_rank)
     # the lattice start compacts to the model's membrane density (~150
     # in-range neighbours per bead) within ~2000 steps: measure that state
     t_eq = time.perf_counter()
     e.step(args.equil)
     t_eq = time.perf_counter() - t_eq
     reach, tune_ms = autotune(e)
+    if args.save_state and rank == 0:
+        save_state(args.save_state, e, n_amp, box, layers, reach)
     e.step(max(args.warmup, 3))
     dist.barrier()
     e.sync()
@@ -321,17 +391,20 @@ def run_engine(args, rank, world, local_rank):
 
     # per-kernel CUDA-event times of un-graphed steps (dominant kernel = force)
     prof = [e.profile_step() for _ in range(5)]
-    force_ms = statistics.median(p_["force"] for p_ in prof)
     kernel_ms = {k: statistics.median(p_[k] for p_ in prof) for k in prof[0]}
+    top = max(PAIR_KERNELS, key=lambda k: kernel_ms[k])
+    kinfo = PAIR_KERNELS[top]
+    top_ms = kernel_ms[top]
     peak, peak_kind = measured_peaks()
-    achieved = FORCE_BYTES_PER_PARTICLE * n / (force_ms * 1e-3) / 1e9
-    traffic = profiled_traffic()
-    roofline = {"kernel": "k_force_f32", "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                "peak_source": f"{peak_kind} copy bandwidth", "force_ms": force_ms,
-                "bytes_per_particle": FORCE_BYTES_PER_PARTICLE,
-                "note": "the force pass is bound by CUDA-core issue (Saru + transcendentals "
-                        "per pair), not by HBM"}
+    achieved = kinfo["bytes_per_particle"] * n / (top_ms * 1e-3) / 1e9
+    roofline = {"kernel": kinfo["kernel"], "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(kinfo["profile"]),
+                "peak_source": f"{peak_kind} copy bandwidth (of {peak_kind})",
+                "kernel_ms": top_ms, "bytes_per_particle": kinfo["bytes_per_particle"],
+                "note": "the pair passes are bound by CUDA-core instruction issue (distance "
+                        "tests, Saru hash, transcendentals per pair), not by HBM; the HBM "
+                        "fraction is small by construction"}
     step_gbs = STEP_BYTES_PER_PARTICLE * n / (ms_max / args.steps * 1e-3) / 1e9
 
     # plain FP64 pair kernels on the same workload (the baseline of the metric)
@@ -339,7 +412,7 @@ def run_engine(args, rank, world, local_rank):
     if not args.no_fp64:
         eq = e.download()
         st64 = dict(st, pos=eq["pos"], vel=eq["vel"], acc=eq["acc"])
-        e64 = make_engine(st64, n_amp, rp, flags=CFG_FP64_PAIRS)
+        e64 = make_engine(st64, n_amp, rp, flags=CFG_FP64_PAIRS, device=local_rank)
         e64.step(1)
         k64 = max(2, min(args.steps, 10))
         e64.step(k64)
@@ -373,7 +446,7 @@ def run_engine(args, rank, world, local_rank):
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic", "config": dict(workload_desc(n, n_amp), equilibration_steps=args.equil,
+           "data": "synthetic", "config": dict(workload_desc(n, n_amp, box, layers), equilibration_steps=args.equil,
                                                equilibration_s=t_eq, cell_reach=reach,
                                                autotune_ms_per_step=tune_ms,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
@@ -398,8 +471,18 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--box", type=float, nargs=3, default=list(BOX),
+                    help="periodic box of the stacked-bilayer workload")
+    ap.add_argument("--layers", type=int, default=N_LAYERS, help="bilayers stacked along z")
+    ap.add_argument("--save-state", default=None,
+                    help="write the equilibrated state (npz) for --kernel-case")
+    ap.add_argument("--kernel-case", default=None,
+                    help="load a saved state and run three graph steps (profiling case)")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
+    if args.kernel_case:
+        run_kernel_case(args.kernel_case, local_rank)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
