@@ -75,6 +75,31 @@ class IdpdChemParams(C.Structure):
     ]
 
 
+CHEM_MAX_CORE = 8
+
+
+class IdpdChemConfig(C.Structure):
+    _fields_ = [
+        ("p", IdpdChemParams),
+        ("mt_seed", C.c_uint32),
+        ("beg_chem", C.c_uint32),
+        ("n_core", C.c_int32),
+        ("core_ptcl_id", C.c_uint32 * CHEM_MAX_CORE),
+        ("reserve_amp", C.c_int32),
+        ("reserved", C.c_int32 * 3),
+    ]
+
+
+class IdpdChemInfo(C.Structure):
+    _fields_ = [
+        ("n_targets", C.c_int32),
+        ("events", C.c_int32),
+        ("stopped", C.c_int32),
+        ("amp_num", C.c_uint32),
+        ("core_raw", (C.c_double * 9) * CHEM_MAX_CORE),
+    ]
+
+
 class IdpdConfig(C.Structure):
     _fields_ = [
         ("n_replicas", C.c_int32),

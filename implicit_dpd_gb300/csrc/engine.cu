@@ -68,6 +68,15 @@ struct idpd_handle {
   float last_ms = 0.f;
   PairTuning tune{1};
   std::string err;
+  // chemistry (replica 0 of a one-replica handle)
+  bool chem_on = false;
+  idpd_chem_config chem_cfg{};
+  ChemDev* chem = nullptr;        // device, kept across re-layouts (MT state)
+  ChemBuffers chem_buf{};         // scratch, sized with the layout
+  int chem_amp_cap = 0;           // molecule slots of the layout (with reserve)
+  int* chem_flag_host = nullptr;  // pinned: the device's stopped flag
+  size_t chem_buf_total = 0, chem_buf_tcap = 0;  // sizes of the allocated scratch
+  bool chem_stopped = false;
 };
 
 namespace {
@@ -116,6 +125,8 @@ void free_all(idpd_handle* h) {
   h->xfer = nullptr;
   h->cm_cnt = nullptr;
   h->amp_rep = nullptr;
+  h->chem_buf = ChemBuffers{h->chem, nullptr, nullptr, nullptr, nullptr};
+  h->chem_buf_total = h->chem_buf_tcap = 0;
   h->cap = h->ncell_cap = h->nblk_cap = h->n_amp_cap = 0;
 }
 
@@ -265,6 +276,51 @@ int ensure_aux(idpd_handle* h) {
 int pull_to_staging(idpd_handle* h);
 
 // Builds the layout from the staging buffers and uploads everything.
+// Scratch of the reaction event for the current layout, and the layout's
+// capacities in the device record (its MT state is kept).
+int chem_layout(idpd_handle* h) {
+  const RepDev& R = h->reps_h[0];
+  const int amp_cap = R.n_amp + h->chem_cfg.reserve_amp;
+  const int tcap = std::max(h->chem_cfg.reserve_amp, 1);
+  const int total = std::max(h->chem_cfg.n_core * amp_cap, 1);
+  ChemBuffers& b = h->chem_buf;
+  b.chem = h->chem;
+  int rc = IDPD_OK;
+  if ((size_t)total > h->chem_buf_total) {
+    if ((rc = dalloc(h, &b.flags, (size_t)total))) return rc;
+    if ((rc = dalloc(h, &b.chunk, (size_t)(total + 1023) / 1024))) return rc;
+    h->chem_buf_total = (size_t)total;
+  }
+  if ((size_t)tcap > h->chem_buf_tcap) {
+    if ((rc = dalloc(h, &b.targets, 2 * (size_t)tcap))) return rc;
+    if ((rc = dalloc(h, &b.draws, 25 * (size_t)tcap))) return rc;
+    h->chem_buf_tcap = (size_t)tcap;
+  }
+  h->chem_amp_cap = amp_cap;
+  const int caps[3] = {R.n + 4 * h->chem_cfg.reserve_amp, amp_cap, tcap};
+  const uint32_t amp_num = (uint32_t)R.n_amp;
+  CK(cudaMemcpyAsync(&h->chem->row_cap, caps, sizeof(caps), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(&h->chem->amp_num, &amp_num, sizeof(uint32_t), cudaMemcpyHostToDevice, h->st));
+  std::vector<float> cfb(h->chem_cfg.reserve_amp, (float)h->params[0].cf_b);
+  if (!cfb.empty())
+    CK(cudaMemcpyAsync(h->d.cf_bend + R.amp_off + R.n_amp, cfb.data(), sizeof(float) * cfb.size(),
+                       cudaMemcpyHostToDevice, h->st));
+  return IDPD_OK;
+}
+
+// Particle and molecule counts of replica 0 after device-side growth.
+int sync_counts(idpd_handle* h) {
+  if (!h->chem_on || !h->on_device || h->layout_dirty) return IDPD_OK;
+  RepDev R;
+  CK(cudaMemcpyAsync(&R, h->d.reps, sizeof(RepDev), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->reps_h[0].n = R.n;
+  h->reps_h[0].n_amp = R.n_amp;
+  h->n[0] = R.n;
+  h->n_amp[0] = R.n_amp;
+  return IDPD_OK;
+}
+
 int commit(idpd_handle* h) {
   if (!h->layout_dirty && !h->reps_dirty) return IDPD_OK;
   for (int r = 0; r < h->R; r++)
@@ -277,21 +333,23 @@ int commit(idpd_handle* h) {
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
       fill_repdev(R, h->params[r], h->tune.reach);
+      // a reaction appends molecules on the device: room for them after the rows
+      const int extra_amp = (h->chem_on && r == 0) ? h->chem_cfg.reserve_amp : 0;
       R.row_off = row;
       R.n = h->n[r];
       R.cell_off = cell;
       R.blk_off = blk;
-      R.nblk = (R.n + kRowBlock - 1) / kRowBlock;
+      R.nblk = (R.n + 4 * extra_amp + kRowBlock - 1) / kRowBlock;
       R.n_amp = h->staged[r].n_amp;
       R.amp_off = amp;
       for (int b = 0; b < R.nblk; b++) {
         blk_rep.push_back(r);
         blk_row.push_back(row + b * kRowBlock);
       }
-      row += R.n;
+      row += R.n + 4 * extra_amp;
       cell += R.ncell;
       blk += R.nblk;
-      amp += R.n_amp;
+      amp += R.n_amp + extra_amp;
       if ((long long)row >= (1ll << 27))
         return fail(h, IDPD_ERR_CAPACITY, "more than 2^27 particles in one handle");
       if ((long long)cell >= (1ll << 31) - 1) return fail(h, IDPD_ERR_CAPACITY, "too many cells");
@@ -308,9 +366,9 @@ int commit(idpd_handle* h) {
     // rows: host transposes into SoA staging, one copy per field
     std::vector<double> buf(9 * (size_t)std::max(row, 1));
     std::vector<uint32_t> ub(5 * (size_t)std::max(row, 1));
-    std::vector<uint32_t> topol(4 * (size_t)std::max(amp, 1));
-    std::vector<float> cfb(std::max(amp, 1));
-    std::vector<int> amp_rep(std::max(amp, 1));
+    std::vector<uint32_t> topol(4 * (size_t)std::max(amp, 1), 0u);
+    std::vector<float> cfb(std::max(amp, 1), 0.0f);
+    std::vector<int> amp_rep(std::max(amp, 1), h->R - 1);
     std::vector<uint32_t> time(h->R);
     for (int r = 0; r < h->R; r++) {
       const Staged& s = h->staged[r];
@@ -355,6 +413,10 @@ int commit(idpd_handle* h) {
       CK(cudaMemcpyAsync(h->amp_rep, amp_rep.data(), sizeof(int) * amp, cudaMemcpyHostToDevice, h->st));
     }
     CK(cudaMemcpyAsync(d.rep_time, time.data(), sizeof(uint32_t) * h->R, cudaMemcpyHostToDevice, h->st));
+    if (h->chem_on) {
+      int rc2 = chem_layout(h);
+      if (rc2) return rc2;
+    }
     CK(cudaStreamSynchronize(h->st));
     h->layout_dirty = false;
     h->reps_dirty = true;
@@ -443,6 +505,7 @@ int check_device_error(idpd_handle* h) {
   switch (e) {
     case kErrNonFinite: return fail(h, IDPD_ERR_NONFINITE, "non-finite pair force");
     case kErrComBox: return fail(h, IDPD_ERR_INVALID_ARG, "neighbour centre of mass needs >= 5 cells per axis (box >= 5)");
+    case kErrChemCapacity: return fail(h, IDPD_ERR_CAPACITY, "reaction event exceeds the reserved molecules (idpd_chem_config.reserve_amp)");
     default: return fail(h, IDPD_ERR_STATE, "device error code %d", e);
   }
 }
@@ -450,7 +513,7 @@ int check_device_error(idpd_handle* h) {
 // Cell list over the current positions (no drift).
 void enqueue_cells(idpd_handle* h, bool drift) {
   launch_drift_bin(h->d, h->nblk, drift, h->st);
-  launch_scan(h->d, h->ncell_tot, h->n_tot, h->st);
+  launch_scan(h->d, h->ncell_tot, h->R - 1, h->st);
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
 }
 
@@ -459,13 +522,19 @@ void enqueue_step(idpd_handle* h) {
   DevState d = h->d;  // the step writes no fine-grained side outputs
   d.dqx = d.dqy = d.dqz = nullptr;
   launch_drift_bin(d, h->nblk, true, h->st);
-  launch_scan(d, h->ncell_tot, h->n_tot, h->st);
+  launch_scan(d, h->ncell_tot, h->R - 1, h->st);
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   launch_density(d, h->nblk, fp64, h->tune.reach, h->st);
   launch_force(d, h->nblk, fp64, false, h->tune, h->st);
   launch_bonded_kick(d, h->nblk, true, h->st);
   launch_cmdrift(d, h->nblk, h->R, false, h->st);
-  launch_time_advance(d, h->R, h->st);
+  if (h->chem_on) {
+    launch_chem(d, h->chem_buf, h->reps_h[0].nblk, h->chem_cfg.n_core, h->chem_amp_cap, false,
+                h->st);
+    launch_time_advance(d, h->R, h->st, &h->chem->stop_now);
+  } else {
+    launch_time_advance(d, h->R, h->st);
+  }
 }
 
 int enqueue_reorder(idpd_handle* h) {
@@ -497,6 +566,17 @@ int pull_to_staging(idpd_handle* h) {
     int rc = idpd_download_state(h, r, s.pos.data(), s.vel.data(), s.acc.data(), s.id.data(),
                                  s.prop.data(), s.amp_id.data(), s.unit.data());
     if (rc) return rc;
+    if (h->chem_on && r == 0 && h->n_amp[0] != s.n_amp) {
+      // molecules appended by reactions: MakeGlobalBondedList over the rows
+      const int na = h->n_amp[0];
+      s.topol.resize(4 * (size_t)na, kNone);
+      s.cf_bend.resize(na, (float)h->params[0].cf_b);
+      for (int i = 0; i < n; i++)
+        if (s.amp_id[i] != kNone && s.amp_id[i] >= (uint32_t)s.n_amp && s.amp_id[i] < (uint32_t)na &&
+            s.unit[i] < 4u)
+          s.topol[4 * (size_t)s.amp_id[i] + s.unit[i]] = (uint32_t)i;
+      s.n_amp = na;
+    }
   }
   return IDPD_OK;
 }
@@ -600,6 +680,8 @@ int idpd_destroy(idpd_handle* h) {
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
   free_all(h);
+  if (h->chem) cudaFree(h->chem);
+  if (h->chem_flag_host) cudaFreeHost(h->chem_flag_host);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->st) cudaStreamDestroy(h->st);
@@ -960,6 +1042,8 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   int rc = commit(h);
   if (rc) return rc;
   if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
+  if (h->chem_on && h->chem_stopped)
+    return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num: the run has ended");
   if (!h->graph) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
@@ -976,11 +1060,21 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
       if ((rc = enqueue_reorder(h))) return rc;
       h->steps_since_sort = 0;
     }
+    if (h->chem_on) {  // the reference's loop ends after the step whose event stopped it
+      CK(cudaMemcpyAsync(h->chem_flag_host, &h->chem->stopped, sizeof(int), cudaMemcpyDeviceToHost,
+                         h->st));
+      CK(cudaStreamSynchronize(h->st));
+      if (*h->chem_flag_host) {
+        h->chem_stopped = true;
+        break;
+      }
+    }
   }
   CK(cudaEventRecord(h->ev1, h->st));
   CK(cudaEventSynchronize(h->ev1));
   CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   h->density_valid = false;
+  if ((rc = sync_counts(h))) return rc;
   return check_device_error(h);
 }
 
@@ -1028,7 +1122,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[0], h->st));
   launch_drift_bin(h->d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[1], h->st));
-  launch_scan(h->d, h->ncell_tot, h->n_tot, h->st);
+  launch_scan(h->d, h->ncell_tot, h->R - 1, h->st);
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
   CK(cudaEventRecord(ev[3], h->st));
@@ -1122,6 +1216,111 @@ int idpd_cell_order(idpd_handle* h, int32_t r, uint32_t* cell_of_row, uint32_t* 
   }
   h->density_valid = false;
   return check_device_error(h);
+}
+
+int idpd_set_chem(idpd_handle* h, int32_t r, const idpd_chem_config* cfg) {
+  if (!h || r != 0) return fail(h, IDPD_ERR_INVALID_ARG, "the reaction acts on replica 0");
+  cudaSetDevice(h->device);
+  if (!cfg) {
+    if (h->chem_on) {
+      int rc = pull_to_staging(h);
+      if (rc) return rc;
+      h->chem_on = false;
+      h->chem_stopped = false;
+      h->layout_dirty = true;
+    }
+    return IDPD_OK;
+  }
+  if (h->R != 1) return fail(h, IDPD_ERR_INVALID_ARG, "the reaction needs a one-replica handle");
+  if (!h->params_set[0]) return fail(h, IDPD_ERR_STATE, "set the parameters first");
+  if (cfg->n_core < 0 || cfg->n_core > IDPD_CHEM_MAX_CORE || cfg->reserve_amp < 0)
+    return fail(h, IDPD_ERR_INVALID_ARG, "n_core must be in [0, %d], reserve_amp >= 0",
+                IDPD_CHEM_MAX_CORE);
+  const idpd_chem_params& q = cfg->p;
+  const double vals[6] = {q.p_thresld, q.eps, q.influ_rad, q.influ_hei, q.influ_dep, q.influ_grd};
+  for (double v : vals)
+    if (!std::isfinite(v)) return fail(h, IDPD_ERR_INVALID_ARG, "non-finite reaction parameter");
+  for (int k = 0; k < 3; k++)
+    if (h->params[0].box[k] < 5.0)
+      return fail(h, IDPD_ERR_INVALID_ARG, "the core geometry needs every box side >= 5");
+  if (h->on_device && !h->layout_dirty) {  // keep the current state through the re-layout
+    int rc = sync_counts(h);
+    if (rc) return rc;
+    if ((rc = pull_to_staging(h))) return rc;
+  }
+  if (!h->chem) {
+    CK(cudaMalloc((void**)&h->chem, sizeof(ChemDev)));
+    CK(cudaMallocHost((void**)&h->chem_flag_host, sizeof(int)));
+  }
+  ChemDev c;
+  std::memset(&c, 0, sizeof(c));
+  c.mt[0] = cfg->mt_seed;  // init_genrand (Matsumoto & Nishimura, mt19937ar)
+  for (int i = 1; i < 624; i++) c.mt[i] = 1812433253u * (c.mt[i - 1] ^ (c.mt[i - 1] >> 30)) + (uint32_t)i;
+  c.mti = 624;
+  c.p_thresld = q.p_thresld;
+  c.eps = q.eps;
+  c.influ_rad = q.influ_rad;
+  c.influ_hei = q.influ_hei;
+  c.influ_dep = q.influ_dep;
+  c.influ_grd = q.influ_grd;
+  c.amp_num = (uint32_t)h->n_amp[0];
+  c.max_amp_num = q.max_amp_num;
+  c.beg_chem = cfg->beg_chem;
+  c.n_core = cfg->n_core;
+  for (int k = 0; k < cfg->n_core; k++) c.core_id[k] = cfg->core_ptcl_id[k];
+  c.cf_bend = (float)h->params[0].cf_b;
+  CK(cudaMemcpyAsync(h->chem, &c, sizeof(c), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->chem_cfg = *cfg;
+  h->chem_on = true;
+  h->chem_stopped = false;
+  h->layout_dirty = true;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+int idpd_chem_event(idpd_handle* h, int32_t* cont) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  if (!h->chem_on) return fail(h, IDPD_ERR_STATE, "the reaction is not enabled (idpd_set_chem)");
+  if (h->chem_stopped) return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  enqueue_cells(h, false);
+  launch_chem(h->d, h->chem_buf, h->reps_h[0].nblk, h->chem_cfg.n_core, h->chem_amp_cap, true,
+              h->st);
+  CK(cudaMemcpyAsync(h->chem_flag_host, &h->chem->stopped, sizeof(int), cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->chem_stopped = *h->chem_flag_host != 0;
+  if (cont) *cont = h->chem_stopped ? 0 : 1;
+  h->density_valid = false;
+  if ((rc = sync_counts(h))) return rc;
+  return check_device_error(h);
+}
+
+int idpd_chem_get_info(idpd_handle* h, int32_t r, idpd_chem_info* info, uint32_t* targets,
+                       int32_t cap) {
+  if (!h || r != 0 || !info || cap < 0) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->chem_on || !h->chem) return fail(h, IDPD_ERR_STATE, "the reaction is not enabled");
+  cudaSetDevice(h->device);
+  ChemDev c;
+  CK(cudaMemcpyAsync(&c, h->chem, sizeof(c), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  std::memset(info, 0, sizeof(*info));
+  info->n_targets = c.n_targets;
+  info->events = c.events;
+  info->stopped = c.stopped;
+  info->amp_num = c.amp_num;
+  for (int k = 0; k < IDPD_CHEM_MAX_CORE && k < kChemMaxCore; k++)
+    for (int q = 0; q < 9; q++) info->core_raw[k][q] = c.core_raw[k][q];
+  const int nt = std::min(c.n_targets, cap);
+  if (targets && nt > 0 && h->chem_buf.targets) {
+    CK(cudaMemcpyAsync(targets, h->chem_buf.targets, sizeof(uint32_t) * 2 * nt,
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return IDPD_OK;
 }
 
 }  // extern "C"

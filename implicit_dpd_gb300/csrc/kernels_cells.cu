@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_parts(int* part, int npar
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_finish(int* cnt, int* start, const int* part,
-                                                              int ncell, int n_tot) {
+                                                              int ncell, int n_tot,
+                                                              const RepDev* last) {
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
   const int off = part[blockIdx.x];
 #pragma unroll
@@ -142,15 +143,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_finish(int* cnt, int* sta
       cnt[base + k] = 0;  // ready for the next binning
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) start[ncell] = n_tot;
+  if (blockIdx.x == 0 && threadIdx.x == 0) start[ncell] = last ? last->row_off + last->n : n_tot;
 }
 
-void launch_scan(const DevState& d, int ncell_tot, int n_tot, cudaStream_t st) {
+void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st) {
   const int nb = (ncell_tot + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot);
   k_scan_parts<<<1, kScanThreads, 0, st>>>(d.scan_part, nb);
-  k_scan_finish<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot,
-                                             n_tot);
+  k_scan_finish<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot, 0,
+                                             d.reps + last_rep);
 }
 
 // ------------------------------------------------- scatter / sort / pack
@@ -211,7 +212,7 @@ void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cuda
   const int nb = (ncell + kScanTile - 1) / kScanTile;
   k_scan_tiles<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell);
   k_scan_parts<<<1, kScanThreads, 0, st>>>(part, nb);
-  k_scan_finish<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, n_tot);
+  k_scan_finish<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, n_tot, nullptr);
 }
 
 void launch_cell_sort_raw(uint32_t* perm, const int* start, int ncell, cudaStream_t st) {

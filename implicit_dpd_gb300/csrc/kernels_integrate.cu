@@ -136,6 +136,10 @@ __global__ void k_bonded_fine(DevState d, int n_amp_tot, const int* amp_rep, dou
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= n_amp_tot) return;
   const RepDev* R = d.reps + amp_rep[m];
+  if (m - R->amp_off >= R->n_amp) {  // slot reserved for molecules a reaction may add
+    vir_part[3 * m] = vir_part[3 * m + 1] = vir_part[3 * m + 2] = 0.0;
+    return;
+  }
   uint32_t rows[4];
   int t[4];
 #pragma unroll
@@ -276,13 +280,14 @@ void launch_cmdrift(const DevState& d, int nblk, int R, bool force_now, cudaStre
   k_cm_apply<<<nblk, kRowBlock, 0, st>>>(d, force_now ? 1 : 0);
 }
 
-__global__ void k_time_advance(uint32_t* t, int R) {
+__global__ void k_time_advance(uint32_t* t, int R, const int* skip) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (skip && *skip) return;
   if (r < R) t[r] += 1u;
 }
 
-void launch_time_advance(const DevState& d, int R, cudaStream_t st) {
-  k_time_advance<<<(R + 127) / 128, 128, 0, st>>>(d.rep_time, R);
+void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* skip) {
+  k_time_advance<<<(R + 127) / 128, 128, 0, st>>>(d.rep_time, R, skip);
 }
 
 // ----------------------------------------------------------- utilities

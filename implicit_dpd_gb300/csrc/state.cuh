@@ -61,14 +61,40 @@ struct DevState {
 
 // Error codes written by kernels into DevState::err.
 enum : int { kErrNone = 0, kErrCellOverflow = 1, kErrBadCell = 2, kErrListOverflow = 3,
-             kErrNonFinite = 4, kErrComBox = 5 };
+             kErrNonFinite = 4, kErrComBox = 5, kErrChemCapacity = 6 };
+
+// Device state of ChemManager (chemmanager.hpp:3-282) for replica 0 of a
+// one-replica handle: the MT19937 generator of PS::MT, the Parameter
+// members the event reads, and what the last event did.
+constexpr int kChemMaxCore = 8;
+struct ChemDev {
+  uint32_t mt[624];  // mt19937ar state (raw words) and its read index
+  int mti;
+  int active;        // an event runs in this step
+  int stopped;       // amp_num reached max_amp_num: RandomChemEvent returned false
+  int stop_now;      // the event of this step stopped the run (time is not advanced)
+  double p_thresld, eps, influ_rad, influ_hei, influ_dep, influ_grd;
+  uint32_t amp_num, max_amp_num, beg_chem;
+  int n_core;
+  uint32_t core_id[kChemMaxCore];
+  int core_row[kChemMaxCore];        // storage row of each core particle (-1: absent)
+  double core_raw[kChemMaxCore][9];  // GetCorePos: head pos, hydrophobic cm, hydrophilic cm
+  double core_h[kChemMaxCore][3];    // projected core position (DetermineTargetIdWithCorePos)
+  double core_n[kChemMaxCore][3];    // unit head-to-tail vector
+  int n_targets;     // targets of the last event
+  int events;        // events run
+  int row_cap, amp_cap, target_cap;  // rows, molecules and targets the buffers hold
+  float cf_bend;     // bend coefficient of new molecules (cf_b)
+};
 
 constexpr int kRowBlock = 128;  // rows per block of row-block launches
 constexpr int kNbrCap = 256;    // neighbour-list slots per particle
 
 // kernels_cells.cu
 void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st);
-void launch_scan(const DevState& d, int ncell_tot, int n_tot, cudaStream_t st);
+// start[ncell_tot] = reps[last_rep].row_off + reps[last_rep].n, read on the
+// device (the particle count can grow on the device).
+void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st);
 void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
                               cudaStream_t st);
 void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol,
@@ -98,6 +124,18 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
                   cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
 
+// kernels_chem.cu: one RandomChemEvent (LOCAL_CHEM_EVENT form) on replica 0.
+// force: run regardless of Parameter::time >= beg_chem (fine-grained call).
+struct ChemBuffers {
+  ChemDev* chem;
+  uint8_t* flags;      // [n_core * amp_cap] molecule inside the reaction cone
+  int* chunk;          // [ceil(n_core * amp_cap / 1024)] flags per 1024-chunk
+  uint32_t* targets;   // [2 * target_cap] head, tail storage rows
+  uint32_t* draws;     // [25 * target_cap] MT draws of the placements
+};
+void launch_chem(const DevState& d, const ChemBuffers& b, int nblk, int n_core, int amp_cap,
+                 bool force, cudaStream_t st);
+
 // kernels_integrate.cu
 void launch_bonded_kick(const DevState& d, int nblk, bool kick, cudaStream_t st);
 void launch_bonded_fine(const DevState& d, int n_amp_tot, const int* amp_rep, double* vir_part,
@@ -105,7 +143,9 @@ void launch_bonded_fine(const DevState& d, int n_amp_tot, const int* amp_rep, do
 void launch_kick_only(const DevState& d, int nblk, cudaStream_t st);
 void launch_fq_to_acc(const DevState& d, int nblk, double* press_out, cudaStream_t st);
 void launch_cmdrift(const DevState& d, int nblk, int R, bool force_now, cudaStream_t st);
-void launch_time_advance(const DevState& d, int R, cudaStream_t st);
+// skip (may be null): device flag that, when set, leaves the step counter
+// unchanged (the reference breaks out of its loop before time++).
+void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* skip = nullptr);
 void launch_saru_test(int n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3, int draws,
                       uint32_t* out_u, float* out_n, cudaStream_t st);
 void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n, cudaStream_t st);

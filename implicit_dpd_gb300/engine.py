@@ -10,7 +10,8 @@ import os
 
 import numpy as np
 
-from .abi import STATUS_NAMES, IdpdConfig, IdpdParams, IdpdRunParam, IdpdTuning
+from .abi import (STATUS_NAMES, IdpdChemConfig, IdpdChemInfo, IdpdConfig, IdpdParams,
+                  IdpdRunParam, IdpdTuning)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
@@ -28,7 +29,7 @@ EXPORTS = [
     "idpd_bonded", "idpd_kick", "idpd_remove_cmdrift", "idpd_step", "idpd_sync",
     "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
     "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
-    "idpd_cell_order_noalloc",
+    "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
 ]
 
 _lib = None
@@ -71,6 +72,9 @@ def load(path=LIB_PATH):
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
+    L.idpd_set_chem.argtypes = [H, C.c_int32, C.POINTER(IdpdChemConfig)]
+    L.idpd_chem_event.argtypes = [H, C.POINTER(C.c_int32)]
+    L.idpd_chem_get_info.argtypes = [H, C.c_int32, C.POINTER(IdpdChemInfo), VP, C.c_int32]
     _lib = L
     return L
 
@@ -165,6 +169,35 @@ class Engine:
         """Fills caller-provided (n, 3) float64 arrays, e.g. pinned buffers."""
         self._ck(self.L.idpd_download_state(self.h, replica, _p(pos), _p(vel), _p(acc), None, None,
                                             None, None), "download_dynamics")
+
+    def set_chem(self, chem_params, mt_seed, core_ptcl_id, reserve_amp, beg_chem=100000,
+                 replica=0):
+        """ChemManager(mt_seed) with the Parameter values of chem_params
+        (IdpdChemParams); None disables the reaction."""
+        if chem_params is None:
+            self._ck(self.L.idpd_set_chem(self.h, replica, None), "set_chem")
+            return
+        cfg = IdpdChemConfig(p=chem_params, mt_seed=mt_seed, beg_chem=beg_chem,
+                             n_core=len(core_ptcl_id), reserve_amp=reserve_amp)
+        for k, v in enumerate(core_ptcl_id):
+            cfg.core_ptcl_id[k] = int(v)
+        self._ck(self.L.idpd_set_chem(self.h, replica, C.byref(cfg)), "set_chem")
+
+    def chem_event(self):
+        """One RandomChemEvent; returns False when amp_num reached max_amp_num."""
+        cont = C.c_int32()
+        self._ck(self.L.idpd_chem_event(self.h, C.byref(cont)), "chem_event")
+        return bool(cont.value)
+
+    def chem_info(self, replica=0, max_targets=1 << 16):
+        info = IdpdChemInfo()
+        t = np.zeros(2 * max_targets, np.uint32)
+        self._ck(self.L.idpd_chem_get_info(self.h, replica, C.byref(info), _p(t), max_targets),
+                 "chem_info")
+        nt = min(info.n_targets, max_targets)
+        return {"n_targets": info.n_targets, "events": info.events, "stopped": bool(info.stopped),
+                "amp_num": info.amp_num, "targets": t[: 2 * nt].reshape(-1, 2),
+                "core_raw": np.array([list(r) for r in info.core_raw])}
 
     def set_tuning(self, reach):
         self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach))), "set_tuning")

@@ -176,6 +176,53 @@ int idpd_step(idpd_handle* h, int32_t nsteps);
 /* Blocks until the handle's stream is idle; reports device-side errors. */
 int idpd_sync(idpd_handle* h);
 
+/* ---- chemical reaction (ChemManager, chemmanager.hpp:3-282) -------------- */
+/* RandomChemEvent in its single-node LOCAL_CHEM_EVENT form (the form every
+ * CHEM_MODE build uses, user_defs.h:6-8) on the device, for a handle with one
+ * replica. Each event draws genrand_real1 of the ChemManager's MT19937 stream
+ * for every molecule whose head lies inside a core's reaction cone, converts
+ * the accepted ones into new 4-bead molecules beside them, appends the new
+ * rows (ids, rows and molecule numbers continue the existing ones) and
+ * extends the bonded topology with them. Decisions and the MT stream are
+ * bit-exact with the reference for the same positions and core geometry. */
+#define IDPD_CHEM_MAX_CORE 8
+typedef struct idpd_chem_config {
+  idpd_chem_params p;       /* p_thresld, eps, influ_*, max_amp_num; p.amp_num is
+                               ignored: the molecules of idpd_build_topology count */
+  uint32_t mt_seed;         /* ChemManager(seed): PS::MT::init_genrand (:176-180)   */
+  uint32_t beg_chem;        /* first step with an event (Parameter::beg_chem,
+                               parameter.hpp:254; main.cpp:187)                    */
+  int32_t n_core;           /* core particles (Parameter::core_ptcl_id), <= 8        */
+  uint32_t core_ptcl_id[IDPD_CHEM_MAX_CORE];
+  int32_t reserve_amp;      /* molecules the handle makes room for (4 rows each)     */
+  int32_t reserved[3];
+} idpd_chem_config;
+
+/* Enables (cfg != NULL) or disables (cfg == NULL) the event for replica 0.
+ * While enabled, idpd_step runs one event per step after kick and the
+ * centre-of-mass correction once Parameter::time >= beg_chem
+ * (src/main.cpp:182-196); when amp_num reaches max_amp_num the step loop ends
+ * after that step without advancing time, as the reference's loop breaks, and
+ * further idpd_step calls return IDPD_ERR_STATE. */
+int idpd_set_chem(idpd_handle* h, int32_t replica, const idpd_chem_config* cfg);
+/* One RandomChemEvent on the current state, whatever the step counter
+ * (chemmanager.hpp:244). *cont = 0 when amp_num reached max_amp_num (the
+ * reference's false return), else 1. */
+int idpd_chem_event(idpd_handle* h, int32_t* cont);
+typedef struct idpd_chem_info {
+  int32_t n_targets;        /* molecules converted by the last event                */
+  int32_t events;           /* events run so far                                    */
+  int32_t stopped;          /* amp_num reached max_amp_num                          */
+  uint32_t amp_num;         /* Parameter::amp_num                                   */
+  /* GetCorePos of the last event per core: core position, hydrophobic and
+   * hydrophilic neighbour centres of mass (nei_cm_pos[Hyphob], [Hyphil]) */
+  double core_raw[IDPD_CHEM_MAX_CORE][9];
+} idpd_chem_info;
+/* State of the last event; targets (may be NULL) receives up to cap pairs of
+ * (head, tail) rows of the converted molecules in upload order. */
+int idpd_chem_get_info(idpd_handle* h, int32_t replica, idpd_chem_info* info, uint32_t* targets,
+                       int32_t cap);
+
 /* ---- tuning --------------------------------------------------------------- */
 /* Launch and cell-grid shape of the pair passes. Every choice gives the same
  * results bit for bit (all pair sums are fixed point); only speed changes. */
