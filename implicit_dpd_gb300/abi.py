@@ -90,6 +90,20 @@ class IdpdChemConfig(C.Structure):
     ]
 
 
+class IdpdObservation(C.Structure):
+    _fields_ = [
+        ("time", C.c_uint32),
+        ("replica", C.c_int32),
+        ("n", C.c_int32),
+        ("n_amp", C.c_int32),
+        ("kin_temp", C.c_double * 4),
+        ("pressure", C.c_double * 3),
+        ("diffusion", C.c_double * 3),
+        ("pair_virial", C.c_double * 3),
+        ("bonded_virial", C.c_double * 3),
+    ]
+
+
 class IdpdChemInfo(C.Structure):
     _fields_ = [
         ("n_targets", C.c_int32),

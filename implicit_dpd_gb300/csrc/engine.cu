@@ -77,6 +77,12 @@ struct idpd_handle {
   int* chem_flag_host = nullptr;  // pinned: the device's stopped flag
   size_t chem_buf_total = 0, chem_buf_tcap = 0;  // sizes of the allocated scratch
   bool chem_stopped = false;
+  // observation (Observer) every obs_period steps
+  int obs_period = 0, obs_cap = 0;
+  idpd_observation* obs_rec = nullptr;  // device records, kept across re-layouts
+  int* obs_count = nullptr;
+  ObsBuffers obs_buf{};                 // per-layout scratch (null until needed)
+  cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
 };
 
 namespace {
@@ -117,6 +123,12 @@ void free_all(idpd_handle* h) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
+  if (h->graph_obs) {
+    cudaGraphExecDestroy(h->graph_obs);
+    h->graph_obs = nullptr;
+  }
+  h->obs_buf.part = nullptr;
+  h->obs_buf.mvir = h->obs_buf.mdif = nullptr;
   for (void* p : h->allocs) cudaFree(p);
   h->allocs.clear();
   h->d = DevState{};
@@ -134,6 +146,10 @@ void invalidate_graph(idpd_handle* h) {
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
+  }
+  if (h->graph_obs) {
+    cudaGraphExecDestroy(h->graph_obs);
+    h->graph_obs = nullptr;
   }
 }
 
@@ -255,12 +271,43 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   return IDPD_OK;
 }
 
-int ensure_aux(idpd_handle* h) {
-  if (h->press64) return IDPD_OK;
+// Per-particle virial of the pair pass (fine-grained API and observation).
+int ensure_press(idpd_handle* h) {
+  if (h->d.pqx) return IDPD_OK;
   int rc;
   DevState& d = h->d;
   if ((rc = dalloc(h, &d.pqx, h->cap)) || (rc = dalloc(h, &d.pqy, h->cap)) ||
-      (rc = dalloc(h, &d.pqz, h->cap)) || (rc = dalloc(h, &d.dqx, h->cap)) ||
+      (rc = dalloc(h, &d.pqz, h->cap)))
+    return rc;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+// Scratch of the observation for the current layout.
+int ensure_obs(idpd_handle* h) {
+  int rc = ensure_press(h);
+  if (rc) return rc;
+  ObsBuffers& b = h->obs_buf;
+  if (!b.part) {
+    if ((rc = dalloc(h, &b.part, (size_t)h->nblk_cap)) ||
+        (rc = dalloc(h, &b.mvir, 3 * (size_t)h->n_amp_cap)) ||
+        (rc = dalloc(h, &b.mdif, (size_t)h->n_amp_cap)))
+      return rc;
+    invalidate_graph(h);
+  }
+  b.rec = h->obs_rec;
+  b.count = h->obs_count;
+  b.cap = h->obs_cap;
+  b.period = h->obs_period;
+  return IDPD_OK;
+}
+
+int ensure_aux(idpd_handle* h) {
+  if (h->press64) return IDPD_OK;
+  int rc = ensure_press(h);
+  if (rc) return rc;
+  DevState& d = h->d;
+  if ((rc = dalloc(h, &d.dqx, h->cap)) ||
       (rc = dalloc(h, &d.dqy, h->cap)) || (rc = dalloc(h, &d.dqz, h->cap)) ||
       (rc = dalloc(h, &h->press64, 3 * (size_t)h->cap)) ||
       (rc = dalloc(h, &h->cm64, 6 * (size_t)h->cap)) ||
@@ -275,7 +322,6 @@ int ensure_aux(idpd_handle* h) {
 // (upload order) so that the layout can be rebuilt.
 int pull_to_staging(idpd_handle* h);
 
-// Builds the layout from the staging buffers and uploads everything.
 // Scratch of the reaction event for the current layout, and the layout's
 // capacities in the device record (its MT state is kept).
 int chem_layout(idpd_handle* h) {
@@ -321,6 +367,7 @@ int sync_counts(idpd_handle* h) {
   return IDPD_OK;
 }
 
+// Builds the layout from the staging buffers and uploads everything.
 int commit(idpd_handle* h) {
   if (!h->layout_dirty && !h->reps_dirty) return IDPD_OK;
   for (int r = 0; r < h->R; r++)
@@ -517,7 +564,10 @@ void enqueue_cells(idpd_handle* h, bool drift) {
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
 }
 
-void enqueue_step(idpd_handle* h) {
+// One MD step; `observe` adds the per-particle virial to the pair pass and
+// the observation kernels (the records are written only for replicas whose
+// step counter is due).
+void enqueue_step(idpd_handle* h, bool observe) {
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   DevState d = h->d;  // the step writes no fine-grained side outputs
   d.dqx = d.dqy = d.dqz = nullptr;
@@ -525,12 +575,15 @@ void enqueue_step(idpd_handle* h) {
   launch_scan(d, h->ncell_tot, h->R - 1, h->st);
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   launch_density(d, h->nblk, fp64, h->tune.reach, h->st);
-  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
+  launch_force(d, h->nblk, fp64, observe, h->tune, h->st);
   launch_bonded_kick(d, h->nblk, true, h->st);
+  if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
   launch_cmdrift(d, h->nblk, h->R, false, h->st);
-  if (h->chem_on) {
+  if (h->chem_on)
     launch_chem(d, h->chem_buf, h->reps_h[0].nblk, h->chem_cfg.n_core, h->chem_amp_cap, false,
                 h->st);
+  if (observe) launch_observe(d, h->obs_buf, h->nblk, h->n_amp_tot, h->amp_rep, h->R, h->st);
+  if (h->chem_on) {
     launch_time_advance(d, h->R, h->st, &h->chem->stop_now);
   } else {
     launch_time_advance(d, h->R, h->st);
@@ -681,6 +734,8 @@ int idpd_destroy(idpd_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   free_all(h);
   if (h->chem) cudaFree(h->chem);
+  if (h->obs_rec) cudaFree(h->obs_rec);
+  if (h->obs_count) cudaFree(h->obs_count);
   if (h->chem_flag_host) cudaFreeHost(h->chem_flag_host);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1044,18 +1099,33 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
   if (h->chem_on && h->chem_stopped)
     return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num: the run has ended");
-  if (!h->graph) {
+  std::vector<uint32_t> time;  // step counters, to pick the steps that observe
+  if (h->obs_period > 0) {
+    if ((rc = ensure_obs(h))) return rc;
+    time.resize(h->R);
+    CK(cudaMemcpyAsync(time.data(), h->d.rep_time, sizeof(uint32_t) * h->R, cudaMemcpyDeviceToHost,
+                       h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  for (int variant = 0; variant < (h->obs_period > 0 ? 2 : 1); variant++) {
+    cudaGraphExec_t& ge = variant ? h->graph_obs : h->graph;
+    if (ge) continue;
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(h);
+    enqueue_step(h, variant == 1);
     CK(cudaStreamEndCapture(h->st, &g));
-    cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
   CK(cudaEventRecord(h->ev0, h->st));
   for (int k = 0; k < nsteps; k++) {
-    CK(cudaGraphLaunch(h->graph, h->st));
+    bool observe = false;
+    for (uint32_t& t : time) {
+      observe = observe || (t % (uint32_t)h->obs_period) == 0u;
+      t++;
+    }
+    CK(cudaGraphLaunch(observe ? h->graph_obs : h->graph, h->st));
     if (++h->steps_since_sort >= h->sort_period) {
       if ((rc = enqueue_reorder(h))) return rc;
       h->steps_since_sort = 0;
@@ -1215,6 +1285,106 @@ int idpd_cell_order(idpd_handle* h, int32_t r, uint32_t* cell_of_row, uint32_t* 
     if (perm_out) perm_out[q] = orig[perm[q] - (uint32_t)R.row_off] - (uint32_t)R.row_off;
   }
   h->density_valid = false;
+  return check_device_error(h);
+}
+
+int idpd_set_observe(idpd_handle* h, int32_t period, int32_t capacity) {
+  if (!h || period < 0 || (period > 0 && capacity < 1))
+    return fail(h, IDPD_ERR_INVALID_ARG, "period >= 0 and capacity >= 1 required");
+  cudaSetDevice(h->device);
+  CK(cudaStreamSynchronize(h->st));
+  if (period > 0 && capacity != h->obs_cap) {
+    if (h->obs_rec) cudaFree(h->obs_rec);
+    h->obs_rec = nullptr;
+    CK(cudaMalloc((void**)&h->obs_rec, sizeof(idpd_observation) * (size_t)capacity));
+    if (!h->obs_count) CK(cudaMalloc((void**)&h->obs_count, sizeof(int)));
+    h->obs_cap = capacity;
+  }
+  if (h->obs_count) CK(cudaMemsetAsync(h->obs_count, 0, sizeof(int), h->st));
+  h->obs_period = period;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+int idpd_get_observations(idpd_handle* h, idpd_observation* out, int32_t max, int32_t* n) {
+  if (!h || !n || max < 0 || (max > 0 && !out)) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  *n = 0;
+  if (!h->obs_count) return IDPD_OK;
+  cudaSetDevice(h->device);
+  int cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, h->obs_count, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int have = std::min(cnt, h->obs_cap);
+  std::vector<idpd_observation> rec(have);
+  if (have > 0)
+    CK(cudaMemcpyAsync(rec.data(), h->obs_rec, sizeof(idpd_observation) * have,
+                       cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemsetAsync(h->obs_count, 0, sizeof(int), h->st));
+  CK(cudaStreamSynchronize(h->st));
+  // replicas finish in any order within a step: order by (time, replica)
+  std::stable_sort(rec.begin(), rec.end(), [](const idpd_observation& a, const idpd_observation& b) {
+    return a.time != b.time ? a.time < b.time : a.replica < b.replica;
+  });
+  const int k = std::min(have, max);
+  for (int i = 0; i < k; i++) out[i] = rec[i];
+  *n = k;
+  if (cnt > h->obs_cap || have > max)
+    return fail(h, IDPD_ERR_CAPACITY, "%d observations recorded, %d returned", cnt, k);
+  return IDPD_OK;
+}
+
+int idpd_density_profile(idpd_handle* h, int32_t r, int32_t axis, int32_t nbins, double* out) {
+  if (!h || r < 0 || r >= h->R || axis < 0 || axis > 2 || nbins < 1 || !out)
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  const RepDev& R = h->reps_h[r];
+  unsigned long long* hist = nullptr;
+  CK(cudaMallocAsync((void**)&hist, sizeof(unsigned long long) * 3 * nbins, h->st));
+  CK(cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * 3 * nbins, h->st));
+  launch_density_profile(h->d, r, R.row_off, R.n, axis, nbins, hist, h->st);
+  std::vector<unsigned long long> c(3 * (size_t)nbins);
+  CK(cudaMemcpyAsync(c.data(), hist, sizeof(unsigned long long) * 3 * nbins, cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaFreeAsync(hist, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const double vol = R.box[0] * R.box[1] * R.box[2] / (double)nbins;
+  for (size_t k = 0; k < c.size(); k++) out[k] = (double)c[k] / vol;
+  return check_device_error(h);
+}
+
+int idpd_rdf(idpd_handle* h, int32_t r, int32_t nbins, double r_max, double* out) {
+  if (!h || r < 0 || r >= h->R || nbins < 1 || nbins > 1024 || !out || !(r_max > 0.0 && r_max <= 2.0))
+    return fail(h, IDPD_ERR_INVALID_ARG, "nbins in [1, 1024], r_max in (0, 2] required");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  const RepDev& R = h->reps_h[r];
+  // search cells have side >= 1 / reach: m layers cover r_max
+  const int m = (int)std::ceil(r_max * (double)R.reach - 1e-12);
+  for (int k = 0; k < 3; k++)
+    if (R.nc[k] < 2 * m + 1)
+      return fail(h, IDPD_ERR_INVALID_ARG, "rdf up to %g needs every box side >= %d", r_max,
+                  2 * (int)std::ceil(r_max) + 1);
+  enqueue_cells(h, false);
+  unsigned long long* hist = nullptr;
+  CK(cudaMallocAsync((void**)&hist, sizeof(unsigned long long) * nbins, h->st));
+  CK(cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * nbins, h->st));
+  launch_rdf(h->d, r, R.row_off, R.n, nbins, r_max, m, hist, h->st);
+  std::vector<unsigned long long> c(nbins);
+  CK(cudaMemcpyAsync(c.data(), hist, sizeof(unsigned long long) * nbins, cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaFreeAsync(hist, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->density_valid = false;
+  const double n = (double)R.n, rho = n / (R.box[0] * R.box[1] * R.box[2]);
+  const double pi = 3.14159265358979323846, dr = r_max / nbins;
+  for (int k = 0; k < nbins; k++) {
+    const double r1 = k * dr, r2 = (k + 1) * dr;
+    const double shell = 4.0 / 3.0 * pi * (r2 * r2 * r2 - r1 * r1 * r1);
+    out[k] = n > 0 ? (double)c[k] / (n * rho * shell) : 0.0;
+  }
   return check_device_error(h);
 }
 

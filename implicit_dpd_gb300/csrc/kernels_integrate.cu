@@ -368,4 +368,273 @@ void launch_soa_to_aos(const double* x, const double* y, const double* z, const 
   k_soa_to_aos<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, orig, row0, aos, n);
 }
 
+// ------------------------------------------------------------ observables
+// Observer::KineticTempera, Pressure and Diffusion (observer.hpp:82-178) of
+// the replicas whose step counter is a multiple of the period. Row sums are
+// taken per row block, molecule values per molecule; one block per replica
+// then reduces them in a fixed order, so a record does not depend on timing.
+__device__ __forceinline__ bool obs_due(const DevState& d, int r, int period) {
+  return period > 0 && (d.rep_time[r] % (uint32_t)period) == 0u;
+}
+
+__device__ __forceinline__ double sq3(double x, double y, double z) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+__global__ void __launch_bounds__(kRowBlock) k_obs_rows(DevState d, ObsBuffers b) {
+  __shared__ double sv[5][kRowBlock / 32];
+  __shared__ long long sq[3][kRowBlock / 32];
+  const int r = d.blk_rep[blockIdx.x];
+  if (!obs_due(d, r, b.period)) return;
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  long long q[3] = {0, 0, 0};
+  if (i < R->row_off + R->n) {
+    v[0] = __dmul_rn(d.vx[i], d.vx[i]);
+    v[1] = __dmul_rn(d.vy[i], d.vy[i]);
+    v[2] = __dmul_rn(d.vz[i], d.vz[i]);
+    v[3] = sq3(d.dsx[i], d.dsy[i], d.dsz[i]);
+    // Diffusion's D_sol runs over the rows from amp_num on (observer.hpp:169-170)
+    const uint32_t u = d.orig[i] - (uint32_t)R->row_off;
+    v[4] = u >= (uint32_t)R->n_amp ? v[3] : 0.0;
+    // press of rows that took part in the pair pass (rows a reaction added
+    // in this step start with press 0, chemmanager.hpp:59)
+    const int s = (int)d.rank[i];
+    if (s < d.cell_start[R->cell_off + R->ncell]) {
+      q[0] = d.pqx[s];
+      q[1] = d.pqy[s];
+      q[2] = d.pqz[s];
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) v[k] = __dadd_rn(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+#pragma unroll
+    for (int k = 0; k < 3; k++) q[k] += __shfl_down_sync(0xffffffffu, q[k], o);
+  }
+  if (lane == 0) {
+    for (int k = 0; k < 5; k++) sv[k][w] = v[k];
+    for (int k = 0; k < 3; k++) sq[k][w] = q[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ObsPart P;
+    double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    long long tq[3] = {0, 0, 0};
+    for (int ww = 0; ww < kRowBlock / 32; ww++) {
+      for (int k = 0; k < 5; k++) t[k] = __dadd_rn(t[k], sv[k][ww]);
+      for (int k = 0; k < 3; k++) tq[k] += sq[k][ww];
+    }
+    for (int k = 0; k < 3; k++) {
+      P.v2[k] = t[k];
+      P.pq[k] = tq[k];
+    }
+    P.ds2 = t[3];
+    P.dsol2 = t[4];
+    b.part[blockIdx.x] = P;
+  }
+}
+
+// Bonded virial per molecule (CalcBondBendGlobalCell's d_vir,
+// bdf_calculator.hpp:160-189) of the molecules that took part in the step's
+// bonded pass.
+__global__ void k_obs_bonds(DevState d, ObsBuffers b, int n_amp_tot, const int* amp_rep) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n_amp_tot) return;
+  const int r = amp_rep[m];
+  if (!obs_due(d, r, b.period)) return;
+  const RepDev* R = d.reps + r;
+  double* out = b.mvir + 3 * (size_t)m;
+  if (m - R->amp_off >= R->n_amp) {
+    out[0] = out[1] = out[2] = 0.0;
+    return;
+  }
+  int t[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) t[k] = (int)d.rank[d.topol[4 * (size_t)m + k]];
+  int cx, cy, cz;
+  cell_xyz((int)d.scell[t[0]] - R->cell_off, R->nc, cx, cy, cz);
+  float3 p[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) p[k] = rel_pos(d, R, t[k], cx, cy, cz);
+  float3 F[4], v;
+  chain_forces(p, R->cf_s, d.cf_bend[m], F, &v);
+  out[0] = (double)v.x;
+  out[1] = (double)v.y;
+  out[2] = (double)v.z;
+}
+
+// Diffusion's molecule term (observer.hpp:157-165): the mean delta_sumr of
+// rows 4i .. 4i+3 (upload order), squared.
+__global__ void k_obs_lipid(DevState d, ObsBuffers b, int n_amp_tot, const int* amp_rep) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n_amp_tot) return;
+  const int r = amp_rep[m];
+  if (!obs_due(d, r, b.period)) return;
+  const RepDev* R = d.reps + r;
+  const int a = m - R->amp_off;
+  if (a >= R->n_amp) {
+    b.mdif[m] = 0.0;
+    return;
+  }
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < kAllUnit; k++) {
+    const int u = kAllUnit * a + k;
+    if (u >= R->n) break;
+    const uint32_t i = d.loc[R->row_off + u];
+    s[0] = __dadd_rn(s[0], d.dsx[i]);
+    s[1] = __dadd_rn(s[1], d.dsy[i]);
+    s[2] = __dadd_rn(s[2], d.dsz[i]);
+  }
+  const double inv = (double)kAllUnit;
+  b.mdif[m] = sq3(__ddiv_rn(s[0], inv), __ddiv_rn(s[1], inv), __ddiv_rn(s[2], inv));
+}
+
+// One block per replica: fixed-order reductions and the record.
+constexpr int kObsThreads = 256;
+__global__ void __launch_bounds__(kObsThreads) k_obs_finalize(DevState d, ObsBuffers b) {
+  __shared__ double sh[11][kObsThreads];
+  __shared__ long long shq[3][kObsThreads];
+  const int r = blockIdx.x;
+  if (!obs_due(d, r, b.period)) return;
+  const RepDev* R = d.reps + r;
+  const int t = threadIdx.x;
+  double v[11];
+  long long q[3] = {0, 0, 0};
+  for (int k = 0; k < 11; k++) v[k] = 0.0;
+  for (int k = R->blk_off + t; k < R->blk_off + R->nblk; k += kObsThreads) {
+    const ObsPart& P = b.part[k];
+    for (int c = 0; c < 3; c++) {
+      v[c] = __dadd_rn(v[c], P.v2[c]);
+      q[c] += P.pq[c];
+    }
+    v[3] = __dadd_rn(v[3], P.ds2);
+    v[4] = __dadd_rn(v[4], P.dsol2);
+  }
+  for (int m = R->amp_off + t; m < R->amp_off + R->n_amp; m += kObsThreads) {
+    for (int c = 0; c < 3; c++) v[5 + c] = __dadd_rn(v[5 + c], b.mvir[3 * (size_t)m + c]);
+    v[8] = __dadd_rn(v[8], b.mdif[m]);
+  }
+  for (int k = 0; k < 11; k++) sh[k][t] = v[k];
+  for (int k = 0; k < 3; k++) shq[k][t] = q[k];
+  __syncthreads();
+  for (int w = kObsThreads / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      for (int k = 0; k < 11; k++) sh[k][t] = __dadd_rn(sh[k][t], sh[k][t + w]);
+      for (int k = 0; k < 3; k++) shq[k][t] += shq[k][t + w];
+    }
+    __syncthreads();
+  }
+  if (t != 0) return;
+  idpd_observation o;
+  const double n = (double)R->n;
+  o.time = d.rep_time[r];
+  o.replica = r;
+  o.n = R->n;
+  o.n_amp = R->n_amp;
+  const double ivol = __dmul_rn(__dmul_rn(R->ibox[0], R->ibox[1]), R->ibox[2]);
+  for (int c = 0; c < 3; c++) {
+    o.kin_temp[c] = __ddiv_rn(sh[c][0], n);
+    o.pair_virial[c] = (double)shq[c][0] * kForceUnscale;
+    o.bonded_virial[c] = sh[5 + c][0];
+    o.pressure[c] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(o.pair_virial[c], 0.5), sh[c][0]),
+                                        __dmul_rn(o.bonded_virial[c], 0.5)),
+                              ivol);
+  }
+  o.kin_temp[3] = __ddiv_rn(__dadd_rn(__dadd_rn(o.kin_temp[0], o.kin_temp[1]), o.kin_temp[2]), 3.0);
+  const int sol = R->n - kAllUnit * R->n_amp;
+  o.diffusion[0] = __ddiv_rn(sh[3][0], n);
+  o.diffusion[1] = R->n_amp > 0 ? __ddiv_rn(sh[8][0], (double)R->n_amp) : 0.0;
+  o.diffusion[2] = sol > 0 ? __ddiv_rn(sh[4][0], (double)sol) : 0.0;
+  const int slot = atomicAdd(b.count, 1);
+  if (slot < b.cap) b.rec[slot] = o;
+}
+
+void launch_observe_bonds(const DevState& d, const ObsBuffers& b, int n_amp_tot,
+                          const int* amp_rep, cudaStream_t st) {
+  if (n_amp_tot > 0) k_obs_bonds<<<(n_amp_tot + 127) / 128, 128, 0, st>>>(d, b, n_amp_tot, amp_rep);
+}
+
+void launch_observe(const DevState& d, const ObsBuffers& b, int nblk, int n_amp_tot,
+                    const int* amp_rep, int R, cudaStream_t st) {
+  if (nblk > 0) k_obs_rows<<<nblk, kRowBlock, 0, st>>>(d, b);
+  if (n_amp_tot > 0) k_obs_lipid<<<(n_amp_tot + 127) / 128, 128, 0, st>>>(d, b, n_amp_tot, amp_rep);
+  k_obs_finalize<<<R, kObsThreads, 0, st>>>(d, b);
+}
+
+// Density profile: particles per slab along `axis` and per property.
+__global__ void k_density_profile(DevState d, int r, int row_off, int n, int axis, int nbins,
+                                  unsigned long long* hist) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int i = row_off + k;
+  const RepDev* R = d.reps + r;
+  const double x = axis == 0 ? d.px[i] : (axis == 1 ? d.py[i] : d.pz[i]);
+  int bin = (int)(x * R->ibox[axis] * (double)nbins);
+  bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+  const uint32_t pr = d.prop[i];
+  if (pr < 3u) atomicAdd(hist + 3 * bin + pr, 1ull);
+}
+
+void launch_density_profile(const DevState& d, int r, int row_off, int n, int axis, int nbins,
+                            unsigned long long* hist, cudaStream_t st) {
+  if (n > 0) k_density_profile<<<(n + 255) / 256, 256, 0, st>>>(d, r, row_off, n, axis, nbins, hist);
+}
+
+// Radial distribution: ordered pairs within r_max over the (2m+1)^3 search
+// cells around each particle (FP64 storage positions, minimum image by the
+// cells' periodic shifts). Shared-memory histogram per block.
+constexpr int kRdfMaxBins = 1024;
+__global__ void __launch_bounds__(256) k_rdf(DevState d, int r, int row_off, int n, int nbins,
+                                             double r_max, int m, unsigned long long* hist) {
+  __shared__ unsigned int h[kRdfMaxBins];
+  for (int k = threadIdx.x; k < nbins; k += blockDim.x) h[k] = 0u;
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (k < n) {
+    const int i = row_off + k;
+    const double xi = d.px[i], yi = d.py[i], zi = d.pz[i];
+    int cx, cy, cz;
+    cell_xyz((int)d.key[i] - R->cell_off, R->nc, cx, cy, cz);
+    const double r2max = r_max * r_max, scale = (double)nbins / r_max;
+    for (int dz = -m; dz <= m; dz++) {
+      const int qz = cz + dz, sz = qz < 0 ? -1 : (qz >= R->nc[2] ? 1 : 0);
+      for (int dy = -m; dy <= m; dy++) {
+        const int qy = cy + dy, sy = qy < 0 ? -1 : (qy >= R->nc[1] ? 1 : 0);
+        for (int dx = -m; dx <= m; dx++) {
+          const int qx = cx + dx, sx = qx < 0 ? -1 : (qx >= R->nc[0] ? 1 : 0);
+          const int cell = R->cell_off + ((qz - sz * R->nc[2]) * R->nc[1] + (qy - sy * R->nc[1])) *
+                                             R->nc[0] + (qx - sx * R->nc[0]);
+          const double shx = sx * R->box[0], shy = sy * R->box[1], shz = sz * R->box[2];
+          for (int t = d.cell_start[cell]; t < d.cell_start[cell + 1]; t++) {
+            const uint32_t j = d.perm[t];
+            if ((int)j == i) continue;
+            const double ex = xi - (d.px[j] + shx), ey = yi - (d.py[j] + shy),
+                         ez = zi - (d.pz[j] + shz);
+            const double dr2 = ex * ex + ey * ey + ez * ez;
+            if (dr2 < r2max) {
+              int bin = (int)(sqrt(dr2) * scale);
+              bin = bin >= nbins ? nbins - 1 : bin;
+              atomicAdd(h + bin, 1u);
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nbins; q += blockDim.x)
+    if (h[q]) atomicAdd(hist + q, (unsigned long long)h[q]);
+}
+
+void launch_rdf(const DevState& d, int r, int row_off, int n, int nbins, double r_max, int m,
+                unsigned long long* hist, cudaStream_t st) {
+  if (n > 0 && nbins > 0 && nbins <= kRdfMaxBins)
+    k_rdf<<<(n + 255) / 256, 256, 0, st>>>(d, r, row_off, n, nbins, r_max, m, hist);
+}
+
 }  // namespace idpd

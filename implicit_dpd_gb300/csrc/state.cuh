@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "idpd_engine.h"
 
 namespace idpd {
 
@@ -135,6 +136,38 @@ struct ChemBuffers {
 };
 void launch_chem(const DevState& d, const ChemBuffers& b, int nblk, int n_core, int amp_cap,
                  bool force, cudaStream_t st);
+
+// Observation of one step (kernels_integrate.cu): per row-block partial sums,
+// per molecule values, then one record per due replica.
+struct ObsPart {
+  double v2[3];     // sum of v_k^2 over the block's rows
+  long long pq[3];  // sum of press_i (the pair pass's 2^-26 fixed point)
+  double ds2;       // sum of |delta_sumr|^2
+  double dsol2;     // the same over rows whose upload index is >= amp_num
+};
+struct ObsBuffers {
+  ObsPart* part;            // [row blocks]
+  double* mvir;             // [molecules * 3] bonded virial per molecule
+  double* mdif;             // [molecules] |mean delta_sumr of rows 4i..4i+3|^2
+  idpd_observation* rec;    // [cap] records
+  int* count;               // records written (may exceed cap: dropped)
+  int cap;
+  int period;
+};
+// Bonded virial per molecule; launched right after the bonded pass (before a
+// reaction event adds molecules).
+void launch_observe_bonds(const DevState& d, const ObsBuffers& b, int n_amp_tot,
+                          const int* amp_rep, cudaStream_t st);
+// Row sums, molecule diffusion and the records; launched after the step's
+// last velocity change, before the step counter advances.
+void launch_observe(const DevState& d, const ObsBuffers& b, int nblk, int n_amp_tot,
+                    const int* amp_rep, int R, cudaStream_t st);
+// Density profile and radial distribution of replica r (counts added to
+// hist, int64 per bin).
+void launch_density_profile(const DevState& d, int r, int row_off, int n, int axis, int nbins,
+                            unsigned long long* hist, cudaStream_t st);
+void launch_rdf(const DevState& d, int r, int row_off, int n, int nbins, double r_max, int m,
+                unsigned long long* hist, cudaStream_t st);
 
 // kernels_integrate.cu
 void launch_bonded_kick(const DevState& d, int nblk, bool kick, cudaStream_t st);

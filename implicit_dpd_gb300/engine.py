@@ -10,8 +10,8 @@ import os
 
 import numpy as np
 
-from .abi import (STATUS_NAMES, IdpdChemConfig, IdpdChemInfo, IdpdConfig, IdpdParams,
-                  IdpdRunParam, IdpdTuning)
+from .abi import (STATUS_NAMES, IdpdChemConfig, IdpdChemInfo, IdpdConfig, IdpdObservation,
+                  IdpdParams, IdpdRunParam, IdpdTuning)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
@@ -30,6 +30,7 @@ EXPORTS = [
     "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
     "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
+    "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
 ]
 
 _lib = None
@@ -75,6 +76,10 @@ def load(path=LIB_PATH):
     L.idpd_set_chem.argtypes = [H, C.c_int32, C.POINTER(IdpdChemConfig)]
     L.idpd_chem_event.argtypes = [H, C.POINTER(C.c_int32)]
     L.idpd_chem_get_info.argtypes = [H, C.c_int32, C.POINTER(IdpdChemInfo), VP, C.c_int32]
+    L.idpd_set_observe.argtypes = [H, C.c_int32, C.c_int32]
+    L.idpd_get_observations.argtypes = [H, VP, C.c_int32, C.POINTER(C.c_int32)]
+    L.idpd_density_profile.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, D]
+    L.idpd_rdf.argtypes = [H, C.c_int32, C.c_int32, C.c_double, D]
     _lib = L
     return L
 
@@ -198,6 +203,35 @@ class Engine:
         return {"n_targets": info.n_targets, "events": info.events, "stopped": bool(info.stopped),
                 "amp_num": info.amp_num, "targets": t[: 2 * nt].reshape(-1, 2),
                 "core_raw": np.array([list(r) for r in info.core_raw])}
+
+    def set_observe(self, period, capacity=4096):
+        """Observer records every `period` steps (0: off)."""
+        self._ck(self.L.idpd_set_observe(self.h, period, capacity), "set_observe")
+
+    def observations(self, max_records=1 << 16):
+        """Drains the recorded observations: a list of dicts, oldest first."""
+        buf = (IdpdObservation * max_records)()
+        n = C.c_int32()
+        self._ck(self.L.idpd_get_observations(self.h, C.cast(buf, C.c_void_p), max_records,
+                                              C.byref(n)), "observations")
+        out = []
+        for o in buf[: n.value]:
+            out.append({"time": o.time, "replica": o.replica, "n": o.n, "n_amp": o.n_amp,
+                        "kin_temp": np.array(o.kin_temp[:]), "pressure": np.array(o.pressure[:]),
+                        "diffusion": np.array(o.diffusion[:]),
+                        "pair_virial": np.array(o.pair_virial[:]),
+                        "bonded_virial": np.array(o.bonded_virial[:])})
+        return out
+
+    def density_profile(self, axis=2, nbins=64, replica=0):
+        out = np.zeros(3 * nbins)
+        self._ck(self.L.idpd_density_profile(self.h, replica, axis, nbins, out), "density_profile")
+        return out.reshape(nbins, 3)
+
+    def rdf(self, nbins=100, r_max=2.0, replica=0):
+        out = np.zeros(nbins)
+        self._ck(self.L.idpd_rdf(self.h, replica, nbins, r_max, out), "rdf")
+        return out
 
     def set_tuning(self, reach):
         self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach))), "set_tuning")

@@ -223,6 +223,45 @@ typedef struct idpd_chem_info {
 int idpd_chem_get_info(idpd_handle* h, int32_t replica, idpd_chem_info* info, uint32_t* targets,
                        int32_t cap);
 
+/* ---- observables (Observer, observer.hpp:82-178) ---------------------------- */
+/* One macro observation of a replica, taken at the end of a step whose
+ * Parameter::time is a multiple of the observation period (Parameter::step_mac,
+ * src/main.cpp:198-205), after the kick, the centre-of-mass correction and the
+ * reaction event, from the same quantities the reference's Observer reads. */
+typedef struct idpd_observation {
+  uint32_t time;            /* Parameter::time of the step                        */
+  int32_t replica;
+  int32_t n;                /* particles                                          */
+  int32_t n_amp;            /* molecules (Parameter::amp_num, Observer::NumAmp)   */
+  double kin_temp[4];       /* KineticTempera: <vx^2>, <vy^2>, <vz^2>, their mean   */
+  double pressure[3];       /* Pressure: (sum_i press_i / 2 + sum_i v_i^2 +
+                               bonded_vir / 2) / volume                             */
+  double diffusion[3];      /* Diffusion: D_ptcl, D_lipid, D_sol (mean squared
+                               delta_sumr of particles, of molecule centres over
+                               rows 4i..4i+3, of rows from amp_num on over sol_num) */
+  double pair_virial[3];    /* sum_i press_i of the step's pair pass               */
+  double bonded_virial[3];  /* the step's ForceBonded virial                       */
+} idpd_observation;
+
+/* period > 0: every step whose Parameter::time % period == 0 records one
+ * idpd_observation per replica into a device buffer of `capacity` records
+ * (the pair pass of those steps also sums the per-particle virial); period 0
+ * switches observation off. */
+int idpd_set_observe(idpd_handle* h, int32_t period, int32_t capacity);
+/* Moves up to max recorded observations (oldest first) into out; *n receives
+ * the count. IDPD_ERR_CAPACITY when records were dropped because the buffer
+ * was full (the records that fit are still returned). */
+int idpd_get_observations(idpd_handle* h, idpd_observation* out, int32_t max, int32_t* n);
+
+/* Number density profile of replica r along axis (0, 1, 2) in nbins slabs,
+ * per particle property: out[bin * 3 + prop] = particles / slab volume. */
+int idpd_density_profile(idpd_handle* h, int32_t replica, int32_t axis, int32_t nbins,
+                         double* out);
+/* Radial distribution function of replica r over all particle pairs, nbins
+ * (<= 1024) shells up to r_max (0 < r_max <= 2; every box side >=
+ * 2 ceil(r_max) + 1): out[k] = g(r) of shell k. */
+int idpd_rdf(idpd_handle* h, int32_t replica, int32_t nbins, double r_max, double* out);
+
 /* ---- tuning --------------------------------------------------------------- */
 /* Launch and cell-grid shape of the pair passes. Every choice gives the same
  * results bit for bit (all pair sums are fixed point); only speed changes. */

@@ -14,7 +14,7 @@ import pyoracle as O
 from implicit_dpd_gb300 import build as B
 from implicit_dpd_gb300 import configs
 from implicit_dpd_gb300.abi import (IdpdChemConfig, IdpdChemInfo, IdpdChemParams, IdpdConfig,
-                                    IdpdParams, IdpdRunParam, params_to_dict)
+                                    IdpdObservation, IdpdParams, IdpdRunParam, params_to_dict)
 from implicit_dpd_gb300.engine import EXPORTS, load
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -46,11 +46,12 @@ def test_struct_layouts_match_c():
 #include <stddef.h>
 #include "idpd_engine.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(idpd_params), sizeof(idpd_run_param),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(idpd_params), sizeof(idpd_run_param),
          sizeof(idpd_chem_params), sizeof(idpd_config), offsetof(idpd_params, seed),
          offsetof(idpd_params, cf_m), sizeof(idpd_chem_config),
          offsetof(idpd_chem_config, reserve_amp), sizeof(idpd_chem_info),
-         offsetof(idpd_chem_info, core_raw));
+         offsetof(idpd_chem_info, core_raw), sizeof(idpd_observation),
+         offsetof(idpd_observation, bonded_virial));
   return 0;
 }
 """
@@ -64,7 +65,8 @@ int main(void) {
     want = [C.sizeof(IdpdParams), C.sizeof(IdpdRunParam), C.sizeof(IdpdChemParams),
             C.sizeof(IdpdConfig), IdpdParams.seed.offset, IdpdParams.cf_m.offset,
             C.sizeof(IdpdChemConfig), IdpdChemConfig.reserve_amp.offset, C.sizeof(IdpdChemInfo),
-            IdpdChemInfo.core_raw.offset]
+            IdpdChemInfo.core_raw.offset, C.sizeof(IdpdObservation),
+            IdpdObservation.bonded_virial.offset]
     assert got == want
 
 
