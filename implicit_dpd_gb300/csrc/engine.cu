@@ -837,7 +837,21 @@ int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double
                       const double* acc) {
   if (!h || r < 0 || r >= h->R || !pos || !vel || !acc)
     return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
-  if (!h->on_device || h->layout_dirty) return fail(h, IDPD_ERR_STATE, "upload the state first");
+  if (!h->on_device || h->layout_dirty) {
+    // not on the device yet: the rows wait in the staging buffers
+    Staged& s = h->staged[r];
+    const size_t n = (size_t)h->n[r];
+    if (s.pos.size() != 3 * n) return fail(h, IDPD_ERR_STATE, "upload the state first");
+    const idpd_params& p = h->params[r];
+    for (size_t i = 0; i < 3 * n; i++)
+      if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || !std::isfinite(acc[i]) ||
+          !(pos[i] >= 0.0 && pos[i] <= p.box[i % 3]))
+        return fail(h, IDPD_ERR_INVALID_ARG, "row %zu: position outside the box or non-finite value", i / 3);
+    s.pos.assign(pos, pos + 3 * n);
+    s.vel.assign(vel, vel + 3 * n);
+    s.acc.assign(acc, acc + 3 * n);
+    return IDPD_OK;
+  }
   cudaSetDevice(h->device);
   const RepDev& R = h->reps_h[r];
   const size_t n = (size_t)R.n;

@@ -130,7 +130,8 @@ int idpd_num_particles(const idpd_handle* h, int32_t replica, int32_t* n);
  * driver loop, src/main.cpp:166-184): overwrites pos/vel/acc of the rows of
  * an uploaded replica, in upload order, keeping ids, properties and the
  * topology. Positions outside [0, box] or non-finite values are rejected by
- * the device and reported by the next call. */
+ * the device and reported by the next call (before the first pass after an
+ * upload, they are checked on the host and the staged rows are replaced). */
 int idpd_set_dynamics(idpd_handle* h, int32_t replica, const double* pos, const double* vel,
                       const double* acc);
 /* Any pointer may be NULL to skip that field. Rows come back in the order
