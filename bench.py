@@ -312,7 +312,7 @@ def save_state(path, e, n_amp, box, layers, reach):
              **{k: out[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")})
 
 
-def run_kernel_case(path, device=0):
+def run_kernel_case(path, device=0, reach=0):
     """Three graph-launched steps from a saved equilibrated state: few
     launches before the pair passes, for kernel profiles of one launch."""
     z = np.load(path)
@@ -320,11 +320,12 @@ def run_kernel_case(path, device=0):
     st = {k: z[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")}
     rp = workload(box=box, layers=layers)[2]
     e = make_engine(st, int(z["n_amp"]), rp, device=device)
-    e.set_tuning(int(z["reach"]))
+    reach = reach or int(z["reach"])
+    e.set_tuning(reach)
     e.step(3)
     e.sync()
     print(json.dumps({"kernel_case": workload_name(box, layers), "n_particles": len(st["pos"]),
-                      "steps": 3, "reach": int(z["reach"])}), flush=True)
+                      "steps": 3, "reach": reach}), flush=True)
     e.close()
 
 
@@ -374,7 +375,11 @@ def run_engine(args, rank, world, local_rank):
     t_eq = time.perf_counter()
     e.step(args.equil)
     t_eq = time.perf_counter() - t_eq
-    reach, tune_ms = autotune(e)
+    if args.reach:
+        e.set_tuning(args.reach)
+        reach, tune_ms = args.reach, None
+    else:
+        reach, tune_ms = autotune(e)
     if args.save_state and rank == 0:
         save_state(args.save_state, e, n_amp, box, layers, reach)
     e.step(max(args.warmup, 3))
@@ -478,10 +483,12 @@ def main():
                     help="write the equilibrated state (npz) for --kernel-case")
     ap.add_argument("--kernel-case", default=None,
                     help="load a saved state and run three graph steps (profiling case)")
+    ap.add_argument("--reach", type=int, default=0,
+                    help="cell reach (1 or 2) instead of the autotuned one")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     if args.kernel_case:
-        run_kernel_case(args.kernel_case, local_rank)
+        run_kernel_case(args.kernel_case, local_rank, args.reach)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
