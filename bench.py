@@ -306,6 +306,54 @@ def run_reference(args, rank, world, budget_s=90.0):
     print(json.dumps(out), flush=True)
 
 
+def replicas_bench(steps=20, n_rep=256, device=0):
+    """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
+    A in [-50, -30], B = 25, densities 5-7): all replicas in one handle,
+    one CUDA graph per step, against the same replicas stepped one handle at
+    a time. Returns particle-steps/s of both."""
+    from implicit_dpd_gb300.abi import FORM_WARREN
+    from implicit_dpd_gb300.engine import Engine, derive_params
+
+    reps = configs.mdpd_replicas(n_rep)
+    params = []
+    for r in reps:
+        p = derive_params(configs.run_param(r["box"], dt=0.005, cf_r=3.0))
+        p.seed, p.time, p.form = r["seed"], 1, FORM_WARREN
+        p.warren_a, p.warren_b, p.warren_rd = r["a"], 25.0, 0.75
+        params.append(p)
+    n_tot = sum(len(r["state"]["pos"]) for r in reps)
+    eb = Engine(n_replicas=n_rep, device=device)
+    for k, (r, p) in enumerate(zip(reps, params)):
+        eb.set_params(p, k)
+        eb.upload(r["state"], k)
+    eb.step(3)
+    eb.step(steps)
+    batched = n_tot * steps / (eb.last_step_ms() * 1e-3)
+    eb.close()
+    singles = []
+    for r, p in zip(reps, params):
+        e = Engine(device=device)
+        e.set_params(p)
+        e.upload(r["state"])
+        e.step(3)
+        singles.append(e)
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e in singles:  # one replica after the other, each its own graph launches
+        e.step(steps)
+    t1 = time.perf_counter() - t0
+    one_at_a_time = n_tot * steps / t1
+    for e in singles:
+        e.close()
+    return {"workload": "mdpd_replicas_256", "n_replicas": n_rep, "n_particles": int(n_tot),
+            "steps": steps, "batched": batched, "one_at_a_time": one_at_a_time,
+            "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
+            "description": "256 MDPD liquids (Warren form, A in [-50,-30], B 25, r_d 0.75, "
+                           "densities 5-7, 2k-60k particles log-uniform) in one handle and one "
+                           "graph per step vs one handle per replica stepped in turn"}
+
+
 def save_state(path, e, n_amp, box, layers, reach):
     out = e.download()
     np.savez(path, box=box, layers=layers, n_amp=n_amp, reach=reach, time=e.get_params().time,
@@ -446,6 +494,7 @@ def run_engine(args, rank, world, local_rank):
                "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": k2,
                "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state per step"}
 
+    batched = replicas_bench(device=local_rank) if not args.no_replicas else None
     cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
     n_reorders = args.steps // 100
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -457,6 +506,7 @@ def run_engine(args, rank, world, local_rank):
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
+           "batched_replicas": batched,
            "gpu_launches": args.steps * KERNELS_PER_STEP + n_reorders * KERNELS_PER_REORDER,
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
     if rank == 0:
@@ -476,6 +526,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-replicas", action="store_true")
     ap.add_argument("--box", type=float, nargs=3, default=list(BOX),
                     help="periodic box of the stacked-bilayer workload")
     ap.add_argument("--layers", type=int, default=N_LAYERS, help="bilayers stacked along z")

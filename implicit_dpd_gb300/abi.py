@@ -76,6 +76,7 @@ class IdpdChemParams(C.Structure):
 
 
 CHEM_MAX_CORE = 8
+WALK_DENSITY, WALK_FORCE = 0, 1
 
 
 class IdpdChemConfig(C.Structure):

@@ -132,3 +132,24 @@ def tile(st, box, reps):
     res = {k: np.concatenate(v) for k, v in out.items()}
     res["pos"] = np.ascontiguousarray(res["pos"])
     return res, box * reps
+
+
+def mdpd_replicas(n_rep=256, seed=5, n_min=2000, n_max=60000, rho=(5.0, 7.0), a=(-50.0, -30.0)):
+    """Independent MDPD liquids of uneven size: particle counts log-uniform
+    in [n_min, n_max], densities uniform in rho, Warren's attraction A
+    uniform in a (B = 25, r_d = 0.75), each in a cubic periodic box of its
+    own, uniform random start. Returns a list of dicts with the state, the
+    box, A and a seed per replica."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n_rep):
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        dens = rng.uniform(*rho)
+        side = (n / dens) ** (1.0 / 3.0)
+        box = np.array([side, side, side])
+        pos = rng.random((n, 3)) * box
+        vel = _velocities(rng, n)
+        st = _state(pos, vel, np.full(n, SOLVENT), np.full(n, NONE32), np.full(n, NONE32))
+        out.append({"state": st, "box": box, "a": float(rng.uniform(*a)),
+                    "seed": int(rng.integers(1, 2**31))})
+    return out

@@ -83,6 +83,7 @@ struct idpd_handle {
   int* obs_count = nullptr;
   ObsBuffers obs_buf{};                 // per-layout scratch (null until needed)
   cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
+  WalkState* walks = nullptr;           // FDPS multi-walk buffers (created on first use)
 };
 
 namespace {
@@ -734,6 +735,7 @@ int idpd_destroy(idpd_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   free_all(h);
   if (h->chem) cudaFree(h->chem);
+  if (h->walks) walk_destroy(h->walks);
   if (h->obs_rec) cudaFree(h->obs_rec);
   if (h->obs_count) cudaFree(h->obs_count);
   if (h->chem_flag_host) cudaFreeHost(h->chem_flag_host);
@@ -1308,7 +1310,8 @@ int idpd_set_observe(idpd_handle* h, int32_t period, int32_t capacity) {
   cudaSetDevice(h->device);
   CK(cudaStreamSynchronize(h->st));
   if (period > 0 && capacity != h->obs_cap) {
-    if (h->obs_rec) cudaFree(h->obs_rec);
+    if (h->walks) walk_destroy(h->walks);
+  if (h->obs_rec) cudaFree(h->obs_rec);
     h->obs_rec = nullptr;
     CK(cudaMalloc((void**)&h->obs_rec, sizeof(idpd_observation) * (size_t)capacity));
     if (!h->obs_count) CK(cudaMalloc((void**)&h->obs_count, sizeof(int)));
@@ -1400,6 +1403,39 @@ int idpd_rdf(idpd_handle* h, int32_t r, int32_t nbins, double r_max, double* out
     out[k] = n > 0 ? (double)c[k] / (n * rho * shell) : 0.0;
   }
   return check_device_error(h);
+}
+
+int idpd_dispatch_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_walk,
+                        const void* const* epi, const int32_t* n_epi, const void* const* epj,
+                        const int32_t* n_epj) {
+  if (!h || (kind != IDPD_WALK_DENSITY && kind != IDPD_WALK_FORCE) || n_walk < 0 ||
+      (n_walk > 0 && (!epi || !n_epi || !epj || !n_epj)))
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->params_set[0]) return fail(h, IDPD_ERR_STATE, "set the parameters of replica 0 first");
+  cudaSetDevice(h->device);
+  if (!h->walks) h->walks = walk_create();
+  idpd_params p = h->params[0];
+  if (h->on_device)  // the step counter lives on the device
+    CK(cudaMemcpy(&p.time, h->d.rep_time, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  RepDev R{};
+  fill_repdev(R, p, 1);
+  std::string err;
+  const int rc = walk_dispatch(h->walks, h->st, R, p, kind, tag, n_walk, epi, n_epi, epj, n_epj, err);
+  if (rc) return fail(h, rc, "dispatch_walks: %s", err.c_str());
+  return IDPD_OK;
+}
+
+int idpd_retrieve_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_walk,
+                        const int32_t* ni, void* const* result) {
+  if (!h || (kind != IDPD_WALK_DENSITY && kind != IDPD_WALK_FORCE) || n_walk < 0 ||
+      (n_walk > 0 && (!ni || !result)))
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  if (!h->walks) return fail(h, IDPD_ERR_STATE, "no walks dispatched");
+  cudaSetDevice(h->device);
+  std::string err;
+  const int rc = walk_retrieve(h->walks, kind, tag, n_walk, ni, result, err);
+  if (rc) return fail(h, rc, "retrieve_walks: %s", err.c_str());
+  return IDPD_OK;
 }
 
 int idpd_set_chem(idpd_handle* h, int32_t r, const idpd_chem_config* cfg) {

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "common.cuh"
 #include "idpd_engine.h"
 
@@ -168,6 +170,16 @@ void launch_density_profile(const DevState& d, int r, int row_off, int n, int ax
                             unsigned long long* hist, cudaStream_t st);
 void launch_rdf(const DevState& d, int r, int row_off, int n, int nbins, double r_max, int m,
                 unsigned long long* hist, cudaStream_t st);
+
+// kernels_walks.cu: the FDPS multi-walk passes (buffers per handle).
+struct WalkState;
+WalkState* walk_create();
+void walk_destroy(WalkState* s);
+int walk_dispatch(WalkState* s, cudaStream_t st, const RepDev& R, const idpd_params& p, int kind,
+                  int tag, int n_walk, const void* const* epi, const int32_t* n_epi,
+                  const void* const* epj, const int32_t* n_epj, std::string& err);
+int walk_retrieve(WalkState* s, int kind, int tag, int n_walk, const int32_t* ni,
+                  void* const* result, std::string& err);
 
 // kernels_integrate.cu
 void launch_bonded_kick(const DevState& d, int nblk, bool kick, cudaStream_t st);

@@ -31,7 +31,21 @@ EXPORTS = [
     "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
+    "idpd_dispatch_walks", "idpd_retrieve_walks",
 ]
+
+# The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
+# record types, for the multi-walk interface.
+WALK_DTYPES = {
+    0: (np.dtype([("prop", "<u4"), ("pad", "<u4"), ("pos", "<f8", 3)]),
+        np.dtype([("prop", "<u4"), ("pad", "<u4"), ("pos", "<f8", 3)]),
+        np.dtype([("dens", "<f8", 3), ("nei_pos_sum", "<f8", (2, 3)), ("nei_cnt", "<u4", 2)])),
+    1: (np.dtype([("id", "<u4"), ("prop", "<u4"), ("pos", "<f8", 3), ("vel", "<f8", 3),
+                  ("dens", "<f8", 3)]),
+        np.dtype([("id", "<u4"), ("prop", "<u4"), ("amp_id", "<u4"), ("unit", "<u4"),
+                  ("pos", "<f8", 3), ("vel", "<f8", 3), ("dens", "<f8", 3)]),
+        np.dtype([("acc", "<f8", 3), ("press", "<f8", 3)])),
+}
 
 _lib = None
 
@@ -80,6 +94,8 @@ def load(path=LIB_PATH):
     L.idpd_get_observations.argtypes = [H, VP, C.c_int32, C.POINTER(C.c_int32)]
     L.idpd_density_profile.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, D]
     L.idpd_rdf.argtypes = [H, C.c_int32, C.c_int32, C.c_double, D]
+    L.idpd_dispatch_walks.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP, VP]
+    L.idpd_retrieve_walks.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, VP, VP]
     _lib = L
     return L
 
@@ -231,6 +247,28 @@ class Engine:
     def rdf(self, nbins=100, r_max=2.0, replica=0):
         out = np.zeros(nbins)
         self._ck(self.L.idpd_rdf(self.h, replica, nbins, r_max, out), "rdf")
+        return out
+
+    def dispatch_walks(self, kind, epi, epj, tag=0):
+        """DispatchKernel over walks: epi / epj are lists of record arrays of
+        WALK_DTYPES[kind][0] / [1]."""
+        n = len(epi)
+        self._walk_keep = [np.ascontiguousarray(a) for a in epi] + [np.ascontiguousarray(a) for a in epj]
+        pi = (C.c_void_p * max(n, 1))(*[a.ctypes.data for a in self._walk_keep[:n]])
+        pj = (C.c_void_p * max(n, 1))(*[a.ctypes.data for a in self._walk_keep[n:]])
+        ni = np.array([len(a) for a in epi], np.int32)
+        nj = np.array([len(a) for a in epj], np.int32)
+        self._walk_ni = ni
+        self._ck(self.L.idpd_dispatch_walks(self.h, kind, tag, n, C.cast(pi, C.c_void_p), _p(ni),
+                                            C.cast(pj, C.c_void_p), _p(nj)), "dispatch_walks")
+
+    def retrieve_walks(self, kind, tag=0):
+        """RetrieveKernel: one record array of WALK_DTYPES[kind][2] per walk."""
+        ni = self._walk_ni
+        out = [np.zeros(int(k), WALK_DTYPES[kind][2]) for k in ni]
+        ptrs = (C.c_void_p * max(len(out), 1))(*[a.ctypes.data for a in out])
+        self._ck(self.L.idpd_retrieve_walks(self.h, kind, tag, len(out), _p(ni),
+                                            C.cast(ptrs, C.c_void_p)), "retrieve_walks")
         return out
 
     def set_tuning(self, reach):

@@ -263,6 +263,46 @@ int idpd_density_profile(idpd_handle* h, int32_t replica, int32_t axis, int32_t 
  * 2 ceil(r_max) + 1): out[k] = g(r) of shell k. */
 int idpd_rdf(idpd_handle* h, int32_t replica, int32_t nbins, double r_max, double* out);
 
+/* ---- FDPS multi-walk interface (f_calculator_gpu.cuh:9-21) ---------------- */
+/* The interaction groups ("walks") FDPS hands to a GPU force kernel: i
+ * particles and the j particles it gathered for them (positions already
+ * image-shifted). The structs have the field order and layout of the
+ * reference's EPI/EPJ/RESULT types (ptcl_class.hpp:5-174), so arrays of those
+ * types can be passed as they are. Pass 1 (kind IDPD_WALK_DENSITY) follows
+ * CalcDensity (nbdf_calculator.hpp:11-60), pass 2 (IDPD_WALK_FORCE)
+ * CalcForceEpEpDPD (:63-147) with replica 0's tables, seed and step counter.
+ * Pair decisions are taken on the FP64 positions as the reference takes them;
+ * pair terms are FP32 with 64-bit fixed-point sums. */
+typedef struct idpd_epi_density { uint32_t prop; double pos[3]; } idpd_epi_density;
+typedef struct idpd_epj_density { uint32_t prop; double pos[3]; } idpd_epj_density;
+typedef struct idpd_result_density {
+  double dens[3];
+  double nei_pos_sum[2][3];
+  uint32_t nei_cnt[2];
+} idpd_result_density;
+typedef struct idpd_epi_dpd {
+  uint32_t id, prop;
+  double pos[3], vel[3], dens[3];
+} idpd_epi_dpd;
+typedef struct idpd_epj_dpd {
+  uint32_t id, prop, amp_id, unit;
+  double pos[3], vel[3], dens[3];
+} idpd_epj_dpd;
+typedef struct idpd_result_dpd { double acc[3], press[3]; } idpd_result_dpd;
+enum { IDPD_WALK_DENSITY = 0, IDPD_WALK_FORCE = 1 };
+
+/* DispatchKernel: copies the walks to the device and starts the pass; returns
+ * without waiting. epi[w] / epj[w] point to n_epi[w] / n_epj[w] structs of the
+ * kind's EPI / EPJ type. One dispatch per kind may be in flight; tag is kept
+ * for the matching retrieve. */
+int idpd_dispatch_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_walk,
+                        const void* const* epi, const int32_t* n_epi, const void* const* epj,
+                        const int32_t* n_epj);
+/* RetrieveKernel: waits for the dispatch with this kind and tag and writes
+ * (does not add) the results of walk w's ni[w] i particles to result[w]. */
+int idpd_retrieve_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_walk,
+                        const int32_t* ni, void* const* result);
+
 /* ---- tuning --------------------------------------------------------------- */
 /* Launch and cell-grid shape of the pair passes. Every choice gives the same
  * results bit for bit (all pair sums are fixed point); only speed changes. */
