@@ -91,6 +91,23 @@ class IdpdChemConfig(C.Structure):
     ]
 
 
+class IdpdRunFile(C.Structure):
+    _fields_ = [
+        ("rp", IdpdRunParam),
+        ("init_amp_num", C.c_uint32),
+        ("sol_num", C.c_uint32),
+        ("all_time", C.c_uint32),
+        ("step_mic", C.c_uint32),
+        ("step_mac", C.c_uint32),
+        ("has_chem", C.c_int32),
+        ("chem", IdpdChemParams),
+        ("influ_vol", C.c_double),
+        ("upside_rad", C.c_double),
+        ("n_core", C.c_int32),
+        ("core_amp_id", C.c_uint32 * CHEM_MAX_CORE),
+    ]
+
+
 class IdpdObservation(C.Structure):
     _fields_ = [
         ("time", C.c_uint32),

@@ -83,6 +83,108 @@ def flat_bilayers(box, n_amp, seed, n_layers=1, axis=2, kT=1.0, jitter=0.0):
     return _state(pos, vel, prop, amp_id, unit)
 
 
+def _place(pos_list, base, nv, box):
+    """SetAmphilPartPos (config_maker.cpp:81-95): four beads from base along
+    nv at the bond length, wrapped into the box."""
+    for u in range(ALL_UNIT):
+        p = base + BOND_LENG * u * nv
+        pos_list.append(p - np.floor(p / box) * box)
+
+
+def _sph_line(out, the, center, rad, sign, lip_len, n_max):
+    """MakeSphLine (config_maker.cpp:139-158): one ring of molecules at polar
+    angle the; False once n_max molecules are placed."""
+    q_thick = 0.5 * ALL_UNIT * BOND_LENG
+    prj = rad * np.sin(the)
+    elem = int(2.0 * np.pi / (lip_len / prj)) if prj > 0 else 0
+    if elem == 0:
+        return True
+    d_phi = 2.0 * np.pi / elem
+    for i in range(elem):
+        phi = d_phi * i
+        nv = sign * np.array([np.sin(the) * np.cos(phi), np.sin(the) * np.sin(phi), np.cos(the)])
+        out.append((sign * nv * (rad - sign * q_thick) + center, nv))
+        if len(out) >= n_max:
+            return False
+    return True
+
+
+def _finish(placed, box, seed, kT):
+    rng = np.random.default_rng(seed)
+    pos = []
+    for base, nv in placed:
+        _place(pos, base, nv, box)
+    pos = np.array(pos)
+    n_amp = len(placed)
+    unit = np.tile(np.arange(ALL_UNIT, dtype=np.uint32), n_amp)
+    amp_id = np.repeat(np.arange(n_amp, dtype=np.uint32), ALL_UNIT)
+    prop = np.where(unit < HEAD_UNIT, HYPHIL, HYPHOB).astype(np.uint32)
+    return _state(pos, _velocities(rng, len(pos), kT), prop, amp_id, unit)
+
+
+def sphere_vesicle(box, n_amp, sph_rad, upper_the=180.0, lip_len=0.4, seed=0, kT=1.0):
+    """Spherical bilayer (MakeSphSheet, config_maker.cpp:175-206): rings of
+    molecules on the outer leaflet (radius sph_rad + half thickness, heads
+    out) then the inner one, polar angle up to upper_the degrees, lip_len
+    between neighbours; a remainder fills rings between the inner ones."""
+    box = np.asarray(box, np.float64)
+    if not (0.0 <= sph_rad <= 0.5 * box.min()):
+        raise ValueError("sphere radius is too large for the box")
+    up_the = upper_the * np.pi / 180.0
+    q_thick = 0.5 * ALL_UNIT * BOND_LENG
+    out_rad, in_rad = sph_rad + q_thick, sph_rad - q_thick
+    out_elem, in_elem = int(up_the / (lip_len / out_rad)), int(up_the / (lip_len / in_rad))
+    d_out, d_in = up_the / out_elem, up_the / in_elem
+    center = 0.5 * box
+    placed = []
+    for elem, d, off, rad, sign in ((out_elem, d_out, 0.0, out_rad, -1.0),
+                                    (in_elem, d_in, 0.0, in_rad, 1.0),
+                                    (in_elem, d_in, 0.5, in_rad, 1.0)):
+        for i in range(elem):
+            if len(placed) >= n_amp or not _sph_line(placed, d * (i + off), center, rad, sign,
+                                                     lip_len, n_amp):
+                break
+        if len(placed) >= n_amp:
+            break
+    if len(placed) != n_amp:
+        raise ValueError("too many molecules for the sphere")
+    return _finish(placed, box, seed, kT)
+
+
+def cylinder_bilayer(box, n_amp, cyl_r, axis=2, lip_len=0.4, seed=0, kT=1.0):
+    """Cylindrical bilayer along `axis` (MakeCylindSheet, config_maker.cpp:
+    222-257): rings every lip_len along the axis, outer leaflet then inner."""
+    box = np.asarray(box, np.float64)
+    q_thick = 0.5 * ALL_UNIT * BOND_LENG
+    if not (cyl_r >= 0.0 and 2.0 * cyl_r + ALL_UNIT * BOND_LENG < box[axis]):
+        raise ValueError("cylinder radius is too large for the box")
+    out_rad, in_rad = cyl_r + q_thick, cyl_r - q_thick
+    z_elem = int(box[axis] / lip_len)
+    in_elem = int(np.pi / (lip_len / in_rad))
+    placed = []
+    perm = [(axis + 1) % 3, (axis + 2) % 3, axis]  # ring plane, then the axis
+    for elem, rad, sign in ((z_elem, out_rad, -1.0), (z_elem, in_rad, 1.0), (in_elem, out_rad, -1.0)):
+        for i in range(elem):
+            ring = []
+            cent = np.zeros(3)
+            _sph_line(ring, 0.5 * np.pi, cent, rad, sign, lip_len, n_amp - len(placed))
+            for base, nv in ring:  # local frame: ring in (x, y), axis along z
+                b = np.zeros(3)
+                v = np.zeros(3)
+                b[perm[0]], b[perm[1]], b[perm[2]] = base[0], base[1], i * lip_len
+                v[perm[0]], v[perm[1]], v[perm[2]] = nv[0], nv[1], nv[2]
+                b[perm[0]] += 0.5 * box[perm[0]]
+                b[perm[1]] += 0.5 * box[perm[1]]
+                placed.append((b, v))
+            if len(placed) >= n_amp:
+                break
+        if len(placed) >= n_amp:
+            break
+    if len(placed) != n_amp:
+        raise ValueError("too many molecules for the cylinder")
+    return _finish(placed, box, seed, kT)
+
+
 def run_param(box, dt=0.005, cf_r=3.0, cf_s=50.0, cf_b=10.0, cf_b_rigid=None, vbb=0.1, chi=30.0,
               kappa=100.0, rho_co=40.0):
     """run_param.txt values (rounded through float as std::stof does)."""

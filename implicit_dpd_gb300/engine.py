@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from .abi import (STATUS_NAMES, IdpdChemConfig, IdpdChemInfo, IdpdConfig, IdpdObservation,
-                  IdpdParams, IdpdRunParam, IdpdTuning)
+                  IdpdParams, IdpdRunFile, IdpdRunParam, IdpdTuning)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
@@ -31,7 +31,8 @@ EXPORTS = [
     "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
-    "idpd_dispatch_walks", "idpd_retrieve_walks",
+    "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
+    "idpd_write_xyz",
 ]
 
 # The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
@@ -94,6 +95,11 @@ def load(path=LIB_PATH):
     L.idpd_get_observations.argtypes = [H, VP, C.c_int32, C.POINTER(C.c_int32)]
     L.idpd_density_profile.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, D]
     L.idpd_rdf.argtypes = [H, C.c_int32, C.c_int32, C.c_double, D]
+    L.idpd_read_run_param.argtypes = [C.c_char_p, C.POINTER(IdpdRunFile)]
+    L.idpd_read_xyz.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_int32),
+                                C.POINTER(C.c_uint32), VP, VP, VP, VP, VP, VP, VP, VP]
+    L.idpd_write_xyz.argtypes = [C.c_char_p, C.c_int32, C.c_uint32, C.c_int32, VP, VP, VP, VP,
+                                 VP, VP, VP, VP]
     L.idpd_dispatch_walks.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, VP, VP, VP, VP]
     L.idpd_retrieve_walks.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, VP, VP]
     _lib = L
@@ -119,6 +125,42 @@ def derive_params(rp):
     out = IdpdParams()
     check(load().idpd_derive_params(C.byref(rp), C.byref(out)), None, "derive_params")
     return out
+
+
+def read_run_param(path):
+    """run_param.txt as the reference's Parameter::LoadParam reads it."""
+    out = IdpdRunFile()
+    check(load().idpd_read_run_param(os.fsencode(path), C.byref(out)), None, "read_run_param")
+    return out
+
+
+def read_xyz(path, cap=None):
+    """An xyz particle file: (state dict in the engine's upload form, time).
+    cap defaults to the particle count of the header."""
+    if cap is None:
+        with open(path) as f:
+            cap = int(f.readline())
+    n = C.c_int32()
+    t = C.c_uint32()
+    st = {k: np.zeros((cap, 3)) for k in ("pos", "vel", "vel_buf", "acc")}
+    for k in ("id", "prop", "amp_id", "unit"):
+        st[k] = np.zeros(cap, np.uint32)
+    check(load().idpd_read_xyz(os.fsencode(path), cap, C.byref(n), C.byref(t), _p(st["pos"]),
+                               _p(st["vel"]), _p(st["vel_buf"]), _p(st["acc"]), _p(st["id"]),
+                               _p(st["prop"]), _p(st["amp_id"]), _p(st["unit"])), None, "read_xyz")
+    return {k: v[: n.value] for k, v in st.items()}, t.value
+
+
+def write_xyz(path, st, time, append=False):
+    """One frame in the reference's xyz format (vel_buf defaults to vel)."""
+    n = len(st["pos"])
+    a = {k: np.ascontiguousarray(st[k], np.float64) for k in ("pos", "vel", "acc")}
+    vb = st.get("vel_buf")
+    u = {k: np.ascontiguousarray(st[k], np.uint32) for k in ("id", "prop", "amp_id", "unit")}
+    check(load().idpd_write_xyz(os.fsencode(path), int(append), time, n, _p(a["pos"]), _p(a["vel"]),
+                                _p(None if vb is None else np.ascontiguousarray(vb, np.float64)),
+                                _p(a["acc"]), _p(u["id"]), _p(u["prop"]), _p(u["amp_id"]),
+                                _p(u["unit"])), None, "write_xyz")
 
 
 def saru_u32(s1, s2, s3, draws):

@@ -303,6 +303,42 @@ int idpd_dispatch_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_wal
 int idpd_retrieve_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_walk,
                         const int32_t* ni, void* const* result);
 
+/* ---- on-disk formats (host only; no device needed) ------------------------ */
+/* run_param.txt as Parameter::LoadParam reads it (parameter.hpp:352-387,
+ * tags of MatchingTagValues :74-136): one "tag value ..." per line, ';'
+ * starts a comment; reals pass through std::stof (float rounding), integers
+ * through std::stoi. influ_vol + upside_rad, when given, set influ_grd and
+ * influ_rad (CalcInfluGrdAndRad :42-56); otherwise influ_vol follows from
+ * them (CalcInfluVol :58-72). The physics and run tags are required as in the
+ * reference (IDPD_ERR_INVALID_ARG names the missing tag); the reaction tags
+ * are optional here (has_chem = 0 when any is missing). */
+typedef struct idpd_run_file {
+  idpd_run_param rp;        /* box_leng, dt, cf_r, cf_s, cf_b, cf_b_rigid, vbb (0.1 when
+                               absent), chi, kappa, rho_co                             */
+  uint32_t init_amp_num, sol_num, all_time, step_mic, step_mac;
+  int32_t has_chem;
+  idpd_chem_params chem;    /* amp_num = init_amp_num                                  */
+  double influ_vol, upside_rad;
+  int32_t n_core;           /* core_amp_id entries (at most IDPD_CHEM_MAX_CORE kept)   */
+  uint32_t core_amp_id[IDPD_CHEM_MAX_CORE];
+} idpd_run_file;
+int idpd_read_run_param(const char* path, idpd_run_file* out);
+
+/* init_config.xyz / traject.xyz / fin_config.xyz (io_util.hpp:26-31,95-129;
+ * rows of FPDPD::writeAscii / readAscii, ptcl_class.hpp:60-86): "<n>", "time
+ * <t>", then per particle: type letter, pos, id, prop, amp_id, unit, vel,
+ * vel_buf, acc, reals printed with %.15g. idpd_read_xyz reads at most cap rows
+ * (IDPD_ERR_CAPACITY beyond) and checks the header and the row count; any
+ * output pointer may be NULL. idpd_write_xyz appends a frame when append != 0
+ * (traject.xyz); vel_buf NULL writes vel in its place. */
+int idpd_read_xyz(const char* path, int32_t cap, int32_t* n, uint32_t* time, double* pos,
+                  double* vel, double* vel_buf, double* acc, uint32_t* id, uint32_t* prop,
+                  uint32_t* amp_id, uint32_t* unit);
+int idpd_write_xyz(const char* path, int32_t append, uint32_t time, int32_t n, const double* pos,
+                   const double* vel, const double* vel_buf, const double* acc,
+                   const uint32_t* id, const uint32_t* prop, const uint32_t* amp_id,
+                   const uint32_t* unit);
+
 /* ---- tuning --------------------------------------------------------------- */
 /* Launch and cell-grid shape of the pair passes. Every choice gives the same
  * results bit for bit (all pair sums are fixed point); only speed changes. */
