@@ -354,13 +354,14 @@ def replicas_bench(steps=20, n_rep=256, device=0):
                            "graph per step vs one handle per replica stepped in turn"}
 
 
-def save_state(path, e, n_amp, box, layers, reach):
+def save_state(path, e, n_amp, box, layers, tune):
     out = e.download()
-    np.savez(path, box=box, layers=layers, n_amp=n_amp, reach=reach, time=e.get_params().time,
+    np.savez(path, box=box, layers=layers, n_amp=n_amp, reach=tune["reach"], skin=tune["skin"],
+             time=e.get_params().time,
              **{k: out[k] for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")})
 
 
-def run_kernel_case(path, device=0, reach=0):
+def run_kernel_case(path, device=0, reach=0, skin=None):
     """Three graph-launched steps from a saved equilibrated state: few
     launches before the pair passes, for kernel profiles of one launch."""
     z = np.load(path)
@@ -369,11 +370,12 @@ def run_kernel_case(path, device=0, reach=0):
     rp = workload(box=box, layers=layers)[2]
     e = make_engine(st, int(z["n_amp"]), rp, device=device)
     reach = reach or int(z["reach"])
-    e.set_tuning(reach)
+    skin = float(z["skin"]) if skin is None else skin
+    e.set_tuning(reach, skin)
     e.step(3)
     e.sync()
     print(json.dumps({"kernel_case": workload_name(box, layers), "n_particles": len(st["pos"]),
-                      "steps": 3, "reach": reach}), flush=True)
+                      "steps": 3, "reach": reach, "skin": skin}), flush=True)
     e.close()
 
 
@@ -396,18 +398,22 @@ def pinned(shape):
     return t, t.numpy()
 
 
-def autotune(e, steps=3):
-    """Times each cell reach on the current state and keeps the fastest.
-    All choices give bit-identical results (fixed-point sums)."""
+TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.2), (1, 0.3), (1, 0.4)]
+
+
+def autotune(e, steps=20):
+    """Times each (cell reach, skin) on the current state over enough steps
+    to include list rebuilds, and keeps the fastest. The reach does not change
+    results; a skin changes them only by FP32 rounding (pair sets exact)."""
     times = {}
-    for reach in (1, 2):
-        e.set_tuning(reach)
-        e.step(1)
+    for reach, skin in TUNE_CHOICES:
+        e.set_tuning(reach, skin)
+        e.step(2)
         e.step(steps)
-        times[reach] = e.last_step_ms() / steps
-    best = min(times, key=times.get)
-    e.set_tuning(best)
-    return best, times
+        times[f"reach{reach}_skin{skin:g}"] = (e.last_step_ms() / steps, reach, skin)
+    best = min(times, key=lambda k: times[k][0])
+    e.set_tuning(times[best][1], times[best][2])
+    return {"reach": times[best][1], "skin": times[best][2]}, {k: v[0] for k, v in times.items()}
 
 
 def run_engine(args, rank, world, local_rank):
@@ -424,8 +430,8 @@ def run_engine(args, rank, world, local_rank):
     e.step(args.equil)
     t_eq = time.perf_counter() - t_eq
     if args.reach:
-        e.set_tuning(args.reach)
-        reach, tune_ms = args.reach, None
+        e.set_tuning(args.reach, args.skin)
+        reach, tune_ms = {"reach": args.reach, "skin": args.skin}, None
     else:
         reach, tune_ms = autotune(e)
     if args.save_state and rank == 0:
@@ -501,7 +507,7 @@ def run_engine(args, rank, world, local_rank):
            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic", "config": dict(workload_desc(n, n_amp, box, layers), equilibration_steps=args.equil,
-                                               equilibration_s=t_eq, cell_reach=reach,
+                                               equilibration_s=t_eq, tuning=reach,
                                                autotune_ms_per_step=tune_ms,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
@@ -536,10 +542,13 @@ def main():
                     help="load a saved state and run three graph steps (profiling case)")
     ap.add_argument("--reach", type=int, default=0,
                     help="cell reach (1 or 2) instead of the autotuned one")
+    ap.add_argument("--skin", type=float, default=0.0,
+                    help="neighbour-list skin with --reach (0: lists every step)")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     if args.kernel_case:
-        run_kernel_case(args.kernel_case, local_rank, args.reach)
+        run_kernel_case(args.kernel_case, local_rank, args.reach,
+                        args.skin if args.reach else None)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

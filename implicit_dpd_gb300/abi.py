@@ -144,7 +144,7 @@ class IdpdConfig(C.Structure):
 
 
 class IdpdTuning(C.Structure):
-    _fields_ = [("reach", C.c_int32), ("reserved", C.c_int32 * 7)]
+    _fields_ = [("reach", C.c_int32), ("skin", C.c_float), ("reserved", C.c_int32 * 6)]
 
 
 def params_to_dict(p):

@@ -266,6 +266,13 @@ __device__ __forceinline__ double fix_to_double(long long q, double unscale) {
 __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
 
 // Cell coordinates of a replica-local cell index (x fastest).
+// Periodic image of j nearest to i along one axis (the one FDPS gathers:
+// within the search radius 1.2 < L / 2 it is unique): j is taken at xj + s L.
+__device__ __forceinline__ int nearest_image(double xi, double xj, double L) {
+  const double e = xi - xj;
+  return e > 0.5 * L ? 1 : (e < -0.5 * L ? -1 : 0);
+}
+
 __device__ __forceinline__ void cell_xyz(int lc, const int* nc, int& cx, int& cy, int& cz) {
   cx = lc % nc[0];
   const int t = lc / nc[0];

@@ -66,7 +66,8 @@ struct idpd_handle {
   cudaGraphExec_t graph = nullptr;
   int steps_since_sort = 0;
   float last_ms = 0.f;
-  PairTuning tune{1};
+  PairTuning tune{1, 0.0f};
+  bool vl_dirty = true;                 // cells rebuilt outside the step: the kept lists are stale
   std::string err;
   // chemistry (replica 0 of a one-replica handle)
   bool chem_on = false;
@@ -175,13 +176,15 @@ int check_params(idpd_handle* h, const idpd_params* p) {
 // Frame cells have side >= the cutoff (nf = floor(box)); the search grid
 // splits each frame cell into `reach` cells per axis. Positions are stored
 // relative to frame cells, so the search grid never changes a pair term.
-void fill_repdev(RepDev& R, const idpd_params& p, int reach) {
+void fill_repdev(RepDev& R, const idpd_params& p, int reach, float skin) {
+  if (skin > 0.0f) reach = 1;  // kept lists use cells of the cutoff plus the skin
+  const double cut = 1.0 + (double)skin;
   R.reach = reach;
   R.rshift = reach == 2 ? 1 : 0;
   for (int k = 0; k < 3; k++) {
     R.box[k] = p.box[k];
     R.ibox[k] = 1.0 / p.box[k];
-    R.nf[k] = (int)(p.box[k] / 1.0);
+    R.nf[k] = (int)(p.box[k] / cut);
     R.nc[k] = R.nf[k] * reach;
     R.inv_cs[k] = (double)R.nc[k] / p.box[k];
     R.cs[k] = p.box[k] / (double)R.nf[k];
@@ -303,6 +306,52 @@ int ensure_obs(idpd_handle* h) {
   return IDPD_OK;
 }
 
+// Kept neighbour lists (skin > 0): buffers and the rebuild record, which
+// starts with a forced rebuild.
+int ensure_verlet(idpd_handle* h) {
+  if (h->tune.skin <= 0.0f) return IDPD_OK;
+  DevState& d = h->d;
+  if (!d.vl) {
+    int rc;
+    if ((rc = dalloc(h, &d.vl, (size_t)kVerletCap * h->cap)) || (rc = dalloc(h, &d.vn, h->cap)) ||
+        (rc = dalloc(h, &d.drx, h->cap)) || (rc = dalloc(h, &d.dry, h->cap)) ||
+        (rc = dalloc(h, &d.drz, h->cap)) || (rc = dalloc(h, &d.vdev, 1)))
+      return rc;
+  }
+  VerletDev v{};
+  const double skin = h->tune.skin;
+  const double half = 0.5 * skin - 1.0e-5;  // margin for the float displacement test
+  v.thr2 = (float)(half * half);
+  v.rv2 = (float)((1.0 + skin) * (1.0 + skin) + 1.0e-4);
+  v.force = 1;
+  CK(cudaMemcpyAsync(d.vdev, &v, sizeof(v), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->vl_dirty = false;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+// Buffers of the kept lists for the current layout, and a forced rebuild
+// when cells were rebuilt outside the step.
+int ensure_verlet_ready(idpd_handle* h) {
+  if (h->tune.skin <= 0.0f) return IDPD_OK;
+  if (!h->d.vl) return ensure_verlet(h);
+  if (h->vl_dirty) {
+    static const int kOne = 1;
+    CK(cudaMemcpyAsync(&h->d.vdev->force, &kOne, sizeof(int), cudaMemcpyHostToDevice, h->st));
+    h->vl_dirty = false;
+  }
+  return IDPD_OK;
+}
+
+// The next step rebuilds the kept lists (their cells or rows changed).
+int force_list_rebuild(idpd_handle* h) {
+  static const int kOne = 1;
+  if (h->d.vdev) CK(cudaMemcpyAsync(&h->d.vdev->force, &kOne, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  h->vl_dirty = false;
+  return IDPD_OK;
+}
+
 int ensure_aux(idpd_handle* h) {
   if (h->press64) return IDPD_OK;
   int rc = ensure_press(h);
@@ -380,7 +429,7 @@ int commit(idpd_handle* h) {
     std::vector<int> blk_rep, blk_row;
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
-      fill_repdev(R, h->params[r], h->tune.reach);
+      fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
       // a reaction appends molecules on the device: room for them after the rows
       const int extra_amp = (h->chem_on && r == 0) ? h->chem_cfg.reserve_amp : 0;
       R.row_off = row;
@@ -398,8 +447,8 @@ int commit(idpd_handle* h) {
       cell += R.ncell;
       blk += R.nblk;
       amp += R.n_amp + extra_amp;
-      if ((long long)row >= (1ll << 27))
-        return fail(h, IDPD_ERR_CAPACITY, "more than 2^27 particles in one handle");
+      if ((long long)row >= (1ll << 25))  // the sorted row of a list entry has 25 bits
+        return fail(h, IDPD_ERR_CAPACITY, "more than 2^25 particle rows in one handle");
       if ((long long)cell >= (1ll << 31) - 1) return fail(h, IDPD_ERR_CAPACITY, "too many cells");
     }
     h->n_tot = row;
@@ -476,7 +525,7 @@ int commit(idpd_handle* h) {
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
       const RepDev keep = R;
-      fill_repdev(R, h->params[r], h->tune.reach);
+      fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
       R.row_off = keep.row_off; R.n = keep.n; R.cell_off = keep.cell_off; R.blk_off = keep.blk_off;
       R.nblk = keep.nblk; R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
       if (R.ncell != keep.ncell) return fail(h, IDPD_ERR_STATE, "box change alters the cell grid; re-upload the state");
@@ -529,7 +578,7 @@ int retune_cells(idpd_handle* h) {
   for (int r = 0; r < h->R; r++) {
     RepDev& R = h->reps_h[r];
     const RepDev keep = R;
-    fill_repdev(R, h->params[r], h->tune.reach);
+    fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
     R.row_off = keep.row_off; R.n = keep.n; R.blk_off = keep.blk_off; R.nblk = keep.nblk;
     R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
     R.cell_off = cell;
@@ -560,6 +609,7 @@ int check_device_error(idpd_handle* h) {
 
 // Cell list over the current positions (no drift).
 void enqueue_cells(idpd_handle* h, bool drift) {
+  h->vl_dirty = true;
   launch_drift_bin(h->d, h->nblk, drift, h->st);
   launch_scan(h->d, h->ncell_tot, h->R - 1, h->st);
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
@@ -572,10 +622,21 @@ void enqueue_step(idpd_handle* h, bool observe) {
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   DevState d = h->d;  // the step writes no fine-grained side outputs
   d.dqx = d.dqy = d.dqz = nullptr;
-  launch_drift_bin(d, h->nblk, true, h->st);
-  launch_scan(d, h->ncell_tot, h->R - 1, h->st);
-  launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
-  launch_density(d, h->nblk, fp64, h->tune.reach, h->st);
+  const bool verlet = d.vdev && h->tune.skin > 0.0f && !fp64;
+  if (verlet) {  // cells and lists only on rebuild steps
+    const int* gate = &d.vdev->rebuild;
+    launch_drift_disp(d, h->nblk, h->st);
+    launch_vl_decide(d, h->st);
+    launch_bin_gated(d, h->nblk, h->st);
+    launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
+    launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
+    launch_verlet_build(d, h->nblk, h->st);
+  } else {
+    launch_drift_bin(d, h->nblk, true, h->st);
+    launch_scan(d, h->ncell_tot, h->R - 1, h->st);
+    launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
+  }
+  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   launch_force(d, h->nblk, fp64, observe, h->tune, h->st);
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
@@ -865,6 +926,7 @@ int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double
   CK(cudaMemcpy2DAsync(h->xfer + 6, row, acc, w, w, n, cudaMemcpyHostToDevice, h->st));
   launch_set_dynamics(h->d, h->xfer, R.row_off, R.n, R.box[0], R.box[1], R.box[2], h->st);
   h->density_valid = false;
+  h->vl_dirty = true;  // new positions: the kept lists are rebuilt
   return IDPD_OK;
 }
 
@@ -1032,6 +1094,7 @@ int idpd_drift(idpd_handle* h) {
   // the arrival slots of this binning are not used: reset the cell counts
   CK(cudaMemsetAsync(h->d.cell_cnt, 0, sizeof(int) * h->ncell_tot, h->st));
   h->density_valid = false;
+  h->vl_dirty = true;
   return check_device_error(h);
 }
 
@@ -1043,7 +1106,7 @@ int idpd_density(idpd_handle* h) {
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   enqueue_cells(h, false);
-  launch_density(h->d, h->nblk, fp64, h->tune.reach, h->st);
+  launch_density(h->d, h->nblk, fp64, h->tune.reach, false, h->st);
   launch_com(h->d, h->nblk, h->cm64, h->cm_cnt, h->st);
   h->density_valid = true;
   return check_device_error(h);
@@ -1115,6 +1178,7 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
   if (h->chem_on && h->chem_stopped)
     return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num: the run has ended");
+  if ((rc = ensure_verlet_ready(h))) return rc;
   std::vector<uint32_t> time;  // step counters, to pick the steps that observe
   if (h->obs_period > 0) {
     if ((rc = ensure_obs(h))) return rc;
@@ -1174,10 +1238,24 @@ int idpd_sync(idpd_handle* h) {
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
   if (!h || !t) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
   if (t->reach < 1 || t->reach > 2) return fail(h, IDPD_ERR_INVALID_ARG, "reach must be 1 or 2");
+  if (!(t->skin >= 0.0f && t->skin < 1.0f))
+    return fail(h, IDPD_ERR_INVALID_ARG, "skin must be in [0, 1)");
+  for (int r = 0; r < h->R; r++)
+    for (int k = 0; k < 3 && t->skin > 0.0f; k++)
+      if (h->params_set[r] && h->params[r].box[k] < 3.0 * (1.0 + t->skin))
+        return fail(h, IDPD_ERR_INVALID_ARG,
+                    "skin %g needs every box side >= %g (three cells of the cutoff plus skin)",
+                    (double)t->skin, 3.0 * (1.0 + t->skin));
   cudaSetDevice(h->device);
-  const bool changed = t->reach != h->tune.reach;
+  const bool changed = t->reach != h->tune.reach || t->skin != h->tune.skin;
   h->tune.reach = t->reach;
-  if (changed && h->on_device && !h->layout_dirty) return retune_cells(h);
+  h->tune.skin = t->skin;
+  if (changed && h->on_device && !h->layout_dirty) {
+    int rc = retune_cells(h);
+    if (rc) return rc;
+    h->vl_dirty = true;
+    return ensure_verlet(h);
+  }
   return IDPD_OK;
 }
 
@@ -1185,6 +1263,7 @@ int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t) {
   if (!h || !t) return IDPD_ERR_INVALID_ARG;
   std::memset(t, 0, sizeof(*t));
   t->reach = h->tune.reach;
+  t->skin = h->tune.skin;
   return IDPD_OK;
 }
 
@@ -1205,22 +1284,35 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   for (auto& e : ev) CK(cudaEventCreate(&e));
   const char* nm[8] = {"drift_bin", "scan", "scatter_sort_pack", "density", "force",
                        "bonded_kick", "cmdrift", "time"};
+  int rc2 = ensure_verlet_ready(h);
+  if (rc2) return rc2;
+  DevState d = h->d;
+  d.dqx = d.dqy = d.dqz = nullptr;
+  const bool verlet = d.vdev && h->tune.skin > 0.0f && !fp64;
+  const int* gate = verlet ? &d.vdev->rebuild : nullptr;
   CK(cudaEventRecord(ev[0], h->st));
-  launch_drift_bin(h->d, h->nblk, true, h->st);
+  if (verlet) {
+    launch_drift_disp(d, h->nblk, h->st);
+    launch_vl_decide(d, h->st);
+    launch_bin_gated(d, h->nblk, h->st);
+  } else {
+    launch_drift_bin(d, h->nblk, true, h->st);
+  }
   CK(cudaEventRecord(ev[1], h->st));
-  launch_scan(h->d, h->ncell_tot, h->R - 1, h->st);
+  launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
   CK(cudaEventRecord(ev[2], h->st));
-  launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
+  launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
+  if (verlet) launch_verlet_build(d, h->nblk, h->st);
   CK(cudaEventRecord(ev[3], h->st));
-  launch_density(h->d, h->nblk, fp64, h->tune.reach, h->st);
+  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   CK(cudaEventRecord(ev[4], h->st));
-  launch_force(h->d, h->nblk, fp64, false, h->tune, h->st);
+  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_bonded_kick(h->d, h->nblk, true, h->st);
+  launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[6], h->st));
-  launch_cmdrift(h->d, h->nblk, h->R, false, h->st);
+  launch_cmdrift(d, h->nblk, h->R, false, h->st);
   CK(cudaEventRecord(ev[7], h->st));
-  launch_time_advance(h->d, h->R, h->st);
+  launch_time_advance(d, h->R, h->st);
   CK(cudaEventRecord(ev[8], h->st));
   CK(cudaEventSynchronize(ev[8]));
   std::string all;
@@ -1418,7 +1510,7 @@ int idpd_dispatch_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_wal
   if (h->on_device)  // the step counter lives on the device
     CK(cudaMemcpy(&p.time, h->d.rep_time, sizeof(uint32_t), cudaMemcpyDeviceToHost));
   RepDev R{};
-  fill_repdev(R, p, 1);
+  fill_repdev(R, p, 1, 0.0f);
   std::string err;
   const int rc = walk_dispatch(h->walks, h->st, R, p, kind, tag, n_walk, epi, n_epi, epj, n_epj, err);
   if (rc) return fail(h, rc, "dispatch_walks: %s", err.c_str());

@@ -23,14 +23,11 @@ __device__ __forceinline__ int cell_coord(double x, double inv_cs, int nc) {
   return c >= nc ? nc - 1 : c;
 }
 
-// One thread per storage row: optional drift, then cell index and arrival slot.
-__global__ void __launch_bounds__(kRowBlock) k_drift_bin(DevState d, int do_drift) {
-  const int r = d.blk_rep[blockIdx.x];
-  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
-  const RepDev* R = d.reps + r;
-  if (i >= R->row_off + R->n) return;
-  double x = d.px[i], y = d.py[i], z = d.pz[i];
-  if (do_drift) {
+// drift_and_predict of one storage row (driftkick.hpp:6-27); x, y, z hold
+// the row's position on entry and the new one on return.
+__device__ __forceinline__ void drift_row(const DevState& d, const RepDev* R, int i, double& x,
+                                          double& y, double& z) {
+  {
     const double dt = R->dt;
     const double h = __dmul_rn(0.5, dt);
     double p[3] = {x, y, z};
@@ -56,12 +53,84 @@ __global__ void __launch_bounds__(kRowBlock) k_drift_bin(DevState d, int do_drif
     d.py[i] = y;
     d.pz[i] = z;
   }
+}
+
+// One thread per storage row: optional drift, then cell index and arrival slot.
+__global__ void __launch_bounds__(kRowBlock) k_drift_bin(DevState d, int do_drift) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (i >= R->row_off + R->n) return;
+  double x = d.px[i], y = d.py[i], z = d.pz[i];
+  if (do_drift) drift_row(d, R, i, x, y, z);
   const int cx = cell_coord(x, R->inv_cs[0], R->nc[0]);
   const int cy = cell_coord(y, R->inv_cs[1], R->nc[1]);
   const int cz = cell_coord(z, R->inv_cs[2], R->nc[2]);
   const uint32_t key = (uint32_t)(R->cell_off + (cz * R->nc[1] + cy) * R->nc[0] + cx);
   d.key[i] = key;
   d.slot[i] = (uint32_t)atomicAdd(&d.cell_cnt[key], 1);
+}
+
+// Steps that keep the neighbour lists: drift, and the largest squared
+// displacement since the last rebuild (delta_sumr accumulates every drift,
+// unwrapped) into the rebuild record.
+__global__ void __launch_bounds__(kRowBlock) k_drift_disp(DevState d) {
+  __shared__ float wmax[kRowBlock / 32];
+  const int r = d.blk_rep[blockIdx.x];
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  float m = 0.0f;
+  if (i < R->row_off + R->n) {
+    double x = d.px[i], y = d.py[i], z = d.pz[i];
+    drift_row(d, R, i, x, y, z);
+    const uint32_t s = d.rank[i];
+    const double ex = d.dsx[i] - d.drx[s], ey = d.dsy[i] - d.dry[s], ez = d.dsz[i] - d.drz[s];
+    m = (float)(ex * ex + ey * ey + ez * ez);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.0f;
+    for (int w = 0; w < kRowBlock / 32; w++) b = fmaxf(b, wmax[w]);
+    // non-negative floats order like their bit patterns
+    if (b > 0.0f) atomicMax(&d.vdev->maxd2, __float_as_uint(b));
+  }
+}
+
+__global__ void k_vl_decide(VerletDev* v) {
+  if (threadIdx.x != 0) return;
+  const int rb = v->force || __uint_as_float(v->maxd2) > v->thr2;
+  v->rebuild = rb;
+  v->force = 0;
+  v->maxd2 = 0u;
+  v->rebuilds += (unsigned)rb;
+}
+
+// The binning of k_drift_bin on a rebuild step (positions already drifted).
+__global__ void __launch_bounds__(kRowBlock) k_bin_gated(DevState d) {
+  if (!d.vdev->rebuild) return;
+  const int r = d.blk_rep[blockIdx.x];
+  const int i = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (i >= R->row_off + R->n) return;
+  const int cx = cell_coord(d.px[i], R->inv_cs[0], R->nc[0]);
+  const int cy = cell_coord(d.py[i], R->inv_cs[1], R->nc[1]);
+  const int cz = cell_coord(d.pz[i], R->inv_cs[2], R->nc[2]);
+  const uint32_t key = (uint32_t)(R->cell_off + (cz * R->nc[1] + cy) * R->nc[0] + cx);
+  d.key[i] = key;
+  d.slot[i] = (uint32_t)atomicAdd(&d.cell_cnt[key], 1);
+}
+
+void launch_drift_disp(const DevState& d, int nblk, cudaStream_t st) {
+  if (nblk > 0) k_drift_disp<<<nblk, kRowBlock, 0, st>>>(d);
+}
+
+void launch_vl_decide(const DevState& d, cudaStream_t st) { k_vl_decide<<<1, 32, 0, st>>>(d.vdev); }
+
+void launch_bin_gated(const DevState& d, int nblk, cudaStream_t st) {
+  if (nblk > 0) k_bin_gated<<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // ---------------------------------------------------------------- scan
@@ -98,8 +167,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_sums, int& 
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* cnt, int* start, int* part,
-                                                             int ncell) {
+                                                             int ncell, const int* gate) {
   __shared__ int ws[33];
+  if (gate && !*gate) return;
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
   int c[kScanPerThread];
   int sum = 0;
@@ -118,8 +188,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int* cnt, int
   if (threadIdx.x == 0) part[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_parts(int* part, int nparts) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_parts(int* part, int nparts,
+                                                             const int* gate) {
   __shared__ int ws[33];
+  if (gate && !*gate) return;
   int carry = 0;
   for (int b = 0; b < nparts; b += kScanThreads) {
     const int i = b + threadIdx.x;
@@ -133,7 +205,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_parts(int* part, int npar
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_finish(int* cnt, int* start, const int* part,
                                                               int ncell, int n_tot,
-                                                              const RepDev* last) {
+                                                              const RepDev* last,
+                                                              const int* gate) {
+  if (gate && !*gate) return;
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
   const int off = part[blockIdx.x];
 #pragma unroll
@@ -146,16 +220,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_finish(int* cnt, int* sta
   if (blockIdx.x == 0 && threadIdx.x == 0) start[ncell] = last ? last->row_off + last->n : n_tot;
 }
 
-void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st) {
+void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st,
+                 const int* gate) {
   const int nb = (ncell_tot + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot);
-  k_scan_parts<<<1, kScanThreads, 0, st>>>(d.scan_part, nb);
+  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot, gate);
+  k_scan_parts<<<1, kScanThreads, 0, st>>>(d.scan_part, nb, gate);
   k_scan_finish<<<nb, kScanThreads, 0, st>>>(d.cell_cnt, d.cell_start, d.scan_part, ncell_tot, 0,
-                                             d.reps + last_rep);
+                                             d.reps + last_rep, gate);
 }
 
 // ------------------------------------------------- scatter / sort / pack
-__global__ void __launch_bounds__(kRowBlock) k_scatter(DevState d) {
+__global__ void __launch_bounds__(kRowBlock) k_scatter(DevState d, const int* gate) {
+  if (gate && !*gate) return;
   const int r = d.blk_rep[blockIdx.x];
   const int i = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
@@ -166,7 +242,8 @@ __global__ void __launch_bounds__(kRowBlock) k_scatter(DevState d) {
 
 // Rows of one cell in ascending storage row: the order a stable counting
 // sort gives, independent of the arrival order of the atomics.
-__global__ void k_cell_sort(uint32_t* perm, const int* start, int ncell) {
+__global__ void k_cell_sort(uint32_t* perm, const int* start, int ncell, const int* gate) {
+  if (gate && !*gate) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
   const int b = start[c], e = start[c + 1];
@@ -181,27 +258,44 @@ __global__ void k_cell_sort(uint32_t* perm, const int* start, int ncell) {
   }
 }
 
+// Offset of x from its frame cell's origin o, at the periodic image nearest
+// to the cell (a particle that crossed the box edge since the cells were
+// built keeps its old cell). For a particle inside its cell, x - o is exact
+// in FP64 (Sterbenz: x lies in [o, 2o] or o = 0).
+__device__ __forceinline__ double cell_offset(double x, double o, double L) {
+  double v = __dsub_rn(x, o);
+  if (v > 0.5 * L) v = __dsub_rn(v, L);
+  else if (v < -0.5 * L) v = __dadd_rn(v, L);
+  return v;
+}
+
 // One thread per sorted slot: FP32 cell-local position, velocity and ids.
-__global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
+// gate (may be null): when it reads 0 the slots keep their rows and cells
+// of the last rebuild.
+__global__ void __launch_bounds__(kRowBlock) k_pack(DevState d, const int* gate) {
   const int r = d.blk_rep[blockIdx.x];
   const int s = d.blk_row[blockIdx.x] + threadIdx.x;
   const RepDev* R = d.reps + r;
   if (s >= R->row_off + R->n) return;
   const uint32_t i = d.perm[s];
-  d.rank[i] = (uint32_t)s;
-  const uint32_t key = d.key[i];
-  d.scell[s] = key;
+  uint32_t key;
+  if (!gate || *gate) {
+    d.rank[i] = (uint32_t)s;
+    key = d.key[i];
+    d.scell[s] = key;
+  } else {
+    key = d.scell[s];
+  }
   int cx, cy, cz;
   cell_xyz((int)key - R->cell_off, R->nc, cx, cy, cz);
   cx >>= R->rshift;  // frame cell
   cy >>= R->rshift;
   cz >>= R->rshift;
-  // x - cx cs is exact in FP64 (Sterbenz: x lies in [o, 2o] or o = 0); its
-  // float split keeps 48 bits for the near-cutoff pair terms.
+  // the float split keeps 48 bits for the near-cutoff pair terms
   float lx, ly, lz, ex, ey, ez;
-  split_double(__dsub_rn(d.px[i], __dmul_rn((double)cx, R->cs[0])), lx, ex);
-  split_double(__dsub_rn(d.py[i], __dmul_rn((double)cy, R->cs[1])), ly, ey);
-  split_double(__dsub_rn(d.pz[i], __dmul_rn((double)cz, R->cs[2])), lz, ez);
+  split_double(cell_offset(d.px[i], __dmul_rn((double)cx, R->cs[0]), R->box[0]), lx, ex);
+  split_double(cell_offset(d.py[i], __dmul_rn((double)cy, R->cs[1]), R->box[1]), ly, ey);
+  split_double(cell_offset(d.pz[i], __dmul_rn((double)cz, R->cs[2]), R->box[2]), lz, ez);
   d.posf[s] = make_float4(lx, ly, lz, __uint_as_float(d.prop[i]));
   d.poslo[s] = make_float4(ex, ey, ez, 0.0f);
   d.velf[s] = make_float4(__double2float_rn(d.vx[i]), __double2float_rn(d.vy[i]),
@@ -210,13 +304,13 @@ __global__ void __launch_bounds__(kRowBlock) k_pack(DevState d) {
 
 void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cudaStream_t st) {
   const int nb = (ncell + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell);
-  k_scan_parts<<<1, kScanThreads, 0, st>>>(part, nb);
-  k_scan_finish<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, n_tot, nullptr);
+  k_scan_tiles<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, nullptr);
+  k_scan_parts<<<1, kScanThreads, 0, st>>>(part, nb, nullptr);
+  k_scan_finish<<<nb, kScanThreads, 0, st>>>(cnt, start, part, ncell, n_tot, nullptr, nullptr);
 }
 
 void launch_cell_sort_raw(uint32_t* perm, const int* start, int ncell, cudaStream_t st) {
-  if (ncell > 0) k_cell_sort<<<(ncell + 255) / 256, 256, 0, st>>>(perm, start, ncell);
+  if (ncell > 0) k_cell_sort<<<(ncell + 255) / 256, 256, 0, st>>>(perm, start, ncell, nullptr);
 }
 
 // Cell index and arrival slot of rows given as x y z triples (one grid, no
@@ -260,11 +354,12 @@ void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t s
 }
 
 void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
-                              cudaStream_t st) {
+                              cudaStream_t st, const int* gate) {
   if (nblk == 0) return;
-  k_scatter<<<nblk, kRowBlock, 0, st>>>(d);
-  if (stable) k_cell_sort<<<(ncell_tot + 255) / 256, 256, 0, st>>>(d.perm, d.cell_start, ncell_tot);
-  k_pack<<<nblk, kRowBlock, 0, st>>>(d);
+  k_scatter<<<nblk, kRowBlock, 0, st>>>(d, gate);
+  if (stable)
+    k_cell_sort<<<(ncell_tot + 255) / 256, 256, 0, st>>>(d.perm, d.cell_start, ncell_tot, gate);
+  k_pack<<<nblk, kRowBlock, 0, st>>>(d, gate);
 }
 
 // ------------------------------------------------------------- reorder

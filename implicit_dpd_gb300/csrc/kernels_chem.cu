@@ -217,9 +217,11 @@ __global__ void k_chem_geom(DevState d, ChemDev* c) {
           const int tb = d.cell_start[cell], te = d.cell_start[cell + 1];
           for (int t = tb + lane; t < te; t += 32) {
             const uint32_t j = d.perm[t];
-            const double jx = __dadd_rn(d.px[j], __dmul_rn((double)sx, R->box[0]));
-            const double jy = __dadd_rn(d.py[j], __dmul_rn((double)sy, R->box[1]));
-            const double jz = __dadd_rn(d.pz[j], __dmul_rn((double)sz, R->box[2]));
+            // the image nearest to the core (the cells may be those of an
+            // earlier step while neighbour lists are reused)
+            const double jx = __dadd_rn(d.px[j], __dmul_rn((double)nearest_image(xi, d.px[j], R->box[0]), R->box[0]));
+            const double jy = __dadd_rn(d.py[j], __dmul_rn((double)nearest_image(yi, d.py[j], R->box[1]), R->box[1]));
+            const double jz = __dadd_rn(d.pz[j], __dmul_rn((double)nearest_image(zi, d.pz[j], R->box[2]), R->box[2]));
             const double ex = __dsub_rn(xi, jx), ey = __dsub_rn(yi, jy), ez = __dsub_rn(zi, jz);
             const double dr2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
             if (dr2 < kRnC2 && dr2 != 0.0) {
@@ -423,6 +425,7 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_event(DevState d, ChemBuf
   // the targets as rows in upload order (storage rows change at reorders)
   for (int k = tid; k < 2 * nt; k += kChemThreads) b.targets[k] = d.orig[b.targets[k]];
   if (tid == 0) {
+    if (nt > 0 && d.vdev) d.vdev->force = 1;  // new rows: cells and kept lists are rebuilt
     R->n = n0 + 4 * nt;
     R->n_amp += nt;
     c->amp_num = amp0 + (uint32_t)nt;

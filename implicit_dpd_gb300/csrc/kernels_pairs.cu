@@ -25,15 +25,20 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
   return v;
 }
 
-// FP64 squared distance of rows i and j (image shift s * L applied to j),
-// in the reference's operation order (nbdf_calculator.hpp:27-29, 86-87).
+// FP64 squared distance of rows i and j in the reference's operation order
+// (nbdf_calculator.hpp:27-29, 86-87), j shifted to its image nearest to i.
+// The image follows from the positions themselves, so it stays right while
+// the cells are reused between list rebuilds.
 __device__ __forceinline__ double exact_dr2(const DevState& d, const RepDev* R, uint32_t i,
-                                            uint32_t j, int sx, int sy, int sz) {
-  const double jx = __dadd_rn(d.px[j], __dmul_rn((double)sx, R->box[0]));
-  const double jy = __dadd_rn(d.py[j], __dmul_rn((double)sy, R->box[1]));
-  const double jz = __dadd_rn(d.pz[j], __dmul_rn((double)sz, R->box[2]));
-  const double ex = __dsub_rn(d.px[i], jx), ey = __dsub_rn(d.py[i], jy),
-               ez = __dsub_rn(d.pz[i], jz);
+                                            uint32_t j) {
+  const double xi = d.px[i], yi = d.py[i], zi = d.pz[i];
+  const double xj = d.px[j], yj = d.py[j], zj = d.pz[j];
+  const int sx = nearest_image(xi, xj, R->box[0]), sy = nearest_image(yi, yj, R->box[1]),
+            sz = nearest_image(zi, zj, R->box[2]);
+  const double jx = __dadd_rn(xj, __dmul_rn((double)sx, R->box[0]));
+  const double jy = __dadd_rn(yj, __dmul_rn((double)sy, R->box[1]));
+  const double jz = __dadd_rn(zj, __dmul_rn((double)sz, R->box[2]));
+  const double ex = __dsub_rn(xi, jx), ey = __dsub_rn(yi, jy), ez = __dsub_rn(zi, jz);
   return __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
 }
 
@@ -125,14 +130,24 @@ __device__ __forceinline__ PairCode unpack_code(uint32_t c) {
 }
 
 // ------------------------------------------------------------- pass 1
-// In-range neighbour list entry: segment slot g (6 bits), frame offset of the
-// candidate's cell relative to the segment's first frame cell (2 bits), row
-// within the segment (8 bits). kNbrFallback marks a particle whose list did
-// not fit (pass 2 then walks its cells again).
+// Neighbour list entry (32 bits): the candidate's sorted row (25 bits) and
+// its frame cell's offset from the particle's frame cell, dx, dy, dz + 1 in
+// 2 bits each. kNbrFallback marks a particle whose list did not fit (the
+// next pass walks its cells again).
 constexpr uint32_t kNbrFallback = 0xffffu;
+constexpr int kRowBits = 25;
+constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
 
-__device__ __forceinline__ uint16_t nbr_entry(int g, int ddx, int off) {
-  return (uint16_t)(g | (ddx << 6) | (off << 8));
+__device__ __forceinline__ uint32_t make_entry(int t, int dx, int dy, int dz) {
+  return (uint32_t)t | ((uint32_t)(dx + 1) << kRowBits) | ((uint32_t)(dy + 1) << (kRowBits + 2)) |
+         ((uint32_t)(dz + 1) << (kRowBits + 4));
+}
+
+__device__ __forceinline__ void read_entry(uint32_t e, int& t, int& dx, int& dy, int& dz) {
+  t = (int)(e & kRowMask);
+  dx = (int)((e >> kRowBits) & 3u) - 1;
+  dy = (int)((e >> (kRowBits + 2)) & 3u) - 1;
+  dz = (int)((e >> (kRowBits + 4)) & 3u) - 1;
 }
 
 template <int REACH>
@@ -143,21 +158,30 @@ __device__ __forceinline__ int frame_step(int t, const int* b) {
   return k;
 }
 
+// Density weight of one in-range pair, accumulated by the candidate's property.
+__device__ __forceinline__ void add_weight(uint32_t& q0, uint32_t& q1, uint32_t& q2, uint32_t pr,
+                                           uint32_t v) {
+  q0 += pr == 0 ? v : 0u;
+  q1 += pr == 1 ? v : 0u;
+  q2 += pr == 2 ? v : 0u;
+}
 
-// One warp per particle. Phase A sweeps the neighbour segments 32
-// candidates at a time and appends the pairs within the cutoff 1 to a list
-// in shared memory; phase B takes the density weights from that list with
-// every lane busy and copies the list out for pass 2. A particle whose list
-// overflows takes its weights during a second sweep instead.
-template <int REACH>
+// One warp per particle. Without kept lists: phase A sweeps the neighbour
+// segments 32 candidates at a time and appends the pairs within the cutoff
+// 1 to a list in shared memory; phase B takes the density weights from that
+// list with every lane busy and copies the list out for pass 2 (a particle
+// whose list overflows takes its weights during a second sweep). With kept
+// lists (VERLET): one pass over the particle's kept list tests each
+// candidate, adds its weight and appends it to the list of pass 2.
+template <int REACH, bool VERLET>
 __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
-  __shared__ uint32_t lst32[kWarps][kNbrCap / 2];
+  __shared__ uint32_t lst[kWarps][kNbrCap];
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
-  uint16_t* L = reinterpret_cast<uint16_t*>(lst32[wid]);
+  uint32_t* L = lst[wid];
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
@@ -169,109 +193,69 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
   for (int s = s0; s < s_end; s++) {
-    const int cell = (int)d.scell[s];
-    if (cell != cached) {
-      int cx, cy, cz;
-      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
-      __syncwarp();
-      build_segments(S, d, R, cx, cy, cz, lane);
-      __syncwarp();
-      cached = cell;
-    }
     const float4 pi = d.posf[s];
     const uint32_t si = d.perm[s];
     int nl = 0;
-    bool lost = false;
-    // ---- phase A: the pairs within the cutoff 1
-#pragma unroll 1
-    for (int g = 0; g < nseg; g++) {
-      const int tb = S.tb[g], te = S.te[g];
-      if (tb >= te) continue;
-      const int code = S.code[g];
-      int b[2 * REACH];
-#pragma unroll
-      for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
-      const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
-      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
-      for (int t0 = tb; t0 < te; t0 += 32) {
-        const int t = t0 + lane;
-        bool in1 = false, near = false;
-        int ddx = 0;
-        if (t < te && t != s) {
-          const float4 pj = __ldg(d.posf + t);
-          ddx = frame_step<REACH>(t, b);
-          const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
-                      ez = bz - pj.z;
-          const float dr2 = ex * ex + ey * ey + ez * ez;
-          in1 = dr2 < 1.0f;
-          near = fabsf(dr2 - 1.0f) <= kGuard;
-        }
-        // rare: a warp-uniform branch keeps the FP64 recheck out of the
-        // common path (a plain branch would be if-converted)
-        if (__any_sync(0xffffffffu, near)) {
-          if (near) {
-            const PairCode pc = unpack_code(pack_code(fx0 + ddx, code));
-            in1 = exact_dr2(d, R, si, d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
-          }
-        }
-        const uint32_t mask = __ballot_sync(0xffffffffu, in1);
-        const int off = t - tb;
-        if (in1) {
-          const int pos = nl + __popc(mask & lt_mask);
-          if (pos < kNbrCap) L[pos] = nbr_entry(g, ddx, off);
-        }
-        lost |= __any_sync(0xffffffffu, in1 && off > 255);
-        nl += __popc(mask);
-      }
-    }
-    __syncwarp();
-    // ---- phase B: density weights
     uint32_t q0 = 0, q1 = 0, q2 = 0;
-    const bool fits = nl <= kNbrCap && !lost;
-    // weight of one pair; called by every lane together (valid = false for
-    // lanes without a pair) so that the rare FP64 recheck is warp-uniform
-    auto take = [&](bool valid, int t, int dx, int dy, int dz, float4 pj) {
+    // weight of one candidate; called by every lane together (valid = false
+    // for lanes without one) so that the rare FP64 recheck is warp-uniform.
+    // Returns whether the pair lies within the cutoff 1.
+    auto test = [&](bool valid, int t, int dx, int dy, int dz, float4 pj, bool list_known) {
       const float ex = (pi.x - (float)dx * csx) - pj.x;
       const float ey = (pi.y - (float)dy * csy) - pj.y;
       const float ez = (pi.z - (float)dz * csz) - pj.z;
       const float dr2 = ex * ex + ey * ey + ez * ez;
-      bool ind = valid && dr2 < cutd2 && dr2 >= 1.0e-10f;
-      const bool recheck = valid && ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f);
-      if (__any_sync(0xffffffffu, recheck) && recheck) {
-        // image shifts of the pair follow from the frame offsets and the cells
-        int cxi, cyi, czi, cxj, cyj, czj;
-        cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cxi, cyi, czi);
-        cell_xyz((int)d.scell[t] - R->cell_off, R->nc, cxj, cyj, czj);
-        const int rs = R->rshift;
-        const int sx = ((cxi >> rs) + dx - (cxj >> rs)) / R->nf[0];
-        const int sy = ((cyi >> rs) + dy - (cyj >> rs)) / R->nf[1];
-        const int sz = ((czi >> rs) + dz - (czj >> rs)) / R->nf[2];
-        const double e2 = exact_dr2(d, R, si, d.perm[t], sx, sy, sz);
-        ind = e2 < cutd2d && e2 != 0.0;
+      bool in1 = valid && (list_known || dr2 < 1.0f);
+      bool ind = in1 && dr2 < cutd2 && dr2 >= 1.0e-10f;
+      const bool near1 = valid && !list_known && fabsf(dr2 - 1.0f) <= kGuard;
+      const bool near2 = valid && ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f);
+      // rare: the FP64 decisions of the reference near the cutoffs and at
+      // coincident positions (a warp-uniform branch keeps them out of the
+      // common path)
+      if (__any_sync(0xffffffffu, near1 || near2)) {
+        if (near1 || near2) {
+          const double e2 = exact_dr2(d, R, si, d.perm[t]);
+          if (near1) in1 = e2 < 1.0;
+          ind = in1 && (near2 ? (e2 < cutd2d && e2 != 0.0) : (dr2 < cutd2 && dr2 >= 1.0e-10f));
+        }
       }
-      if (ind) {
-        const uint32_t v = dens_weight(dr2, warren, inv_rd, wnorm, pre);
-        const uint32_t pr = fbits(pj.w);
-        q0 += pr == 0 ? v : 0u;
-        q1 += pr == 1 ? v : 0u;
-        q2 += pr == 2 ? v : 0u;
-      }
+      if (ind) add_weight(q0, q1, q2, fbits(pj.w), dens_weight(dr2, warren, inv_rd, wnorm, pre));
+      return in1;
     };
-    if (fits) {
-      for (int k0 = 0; k0 < nl; k0 += 32) {
+    const uint32_t nv = VERLET ? (uint32_t)d.vn[s] : kNbrFallback;
+    bool fits = true;
+    if (VERLET && nv != kNbrFallback) {
+      // ---- the particle's kept list: test, weight and list in one pass
+      const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
+      uint32_t e_next = lane < (int)nv ? vl[lane] : 0u;  // one round ahead
+      for (int k0 = 0; k0 < (int)nv; k0 += 32) {
         const int k = k0 + lane;
-        const bool valid = k < nl;
-        const uint32_t e = valid ? L[k] : 0u;
-        const int g = (int)(e & 63u);
-        const int code = S.code[g];
-        const int t = S.tb[g] + (int)(e >> 8);
-        take(valid, t, (code & 7) - 4 + (int)((e >> 6) & 3u), ((code >> 3) & 7) - 4,
-             ((code >> 6) & 7) - 4, valid ? __ldg(d.posf + t) : pi);
+        const bool valid = k < (int)nv;
+        const uint32_t e = e_next;
+        if (k + 32 < (int)nv) e_next = vl[k + 32];
+        int t, dx, dy, dz;
+        read_entry(e, t, dx, dy, dz);
+        if (!valid) t = s;
+        const bool in1 = test(valid, t, dx, dy, dz, __ldg(d.posf + t), false);
+        const uint32_t mask = __ballot_sync(0xffffffffu, in1);
+        if (in1) {
+          const int pos = nl + __popc(mask & lt_mask);
+          if (pos < kNbrCap) L[pos] = e;
+        }
+        nl += __popc(mask);
       }
-      // list out for pass 2: 4-byte words, coalesced
-      uint32_t* out = reinterpret_cast<uint32_t*>(d.nbl + (size_t)s * kNbrCap);
-      for (int k = lane; k < (nl + 1) / 2; k += 32) out[k] = lst32[wid][k];
+      fits = nl <= kNbrCap;
     } else {
+      const int cell = (int)d.scell[s];
+      if (cell != cached) {
+        int cx, cy, cz;
+        cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+        __syncwarp();
+        build_segments(S, d, R, cx, cy, cz, lane);
+        __syncwarp();
+        cached = cell;
+      }
+      // ---- phase A: the pairs within the cutoff 1
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {
         const int tb = S.tb[g], te = S.te[g];
@@ -281,14 +265,66 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
 #pragma unroll
         for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
         const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+        const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
         for (int t0 = tb; t0 < te; t0 += 32) {
           const int t = t0 + lane;
-          const bool valid = t < te && t != s;
-          take(valid, t, fx0 + frame_step<REACH>(t, b), dy, dz, valid ? __ldg(d.posf + t) : pi);
+          bool in1 = false, near = false;
+          int ddx = 0;
+          if (t < te && t != s) {
+            const float4 pj = __ldg(d.posf + t);
+            ddx = frame_step<REACH>(t, b);
+            const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
+                        ez = bz - pj.z;
+            const float dr2 = ex * ex + ey * ey + ez * ez;
+            in1 = dr2 < 1.0f;
+            near = fabsf(dr2 - 1.0f) <= kGuard;
+          }
+          if (__any_sync(0xffffffffu, near)) {
+            if (near) in1 = exact_dr2(d, R, si, d.perm[t]) < 1.0;
+          }
+          const uint32_t mask = __ballot_sync(0xffffffffu, in1);
+          if (in1) {
+            const int pos = nl + __popc(mask & lt_mask);
+            if (pos < kNbrCap) L[pos] = make_entry(t, fx0 + ddx, dy, dz);
+          }
+          nl += __popc(mask);
+        }
+      }
+      __syncwarp();
+      fits = nl <= kNbrCap;
+      // ---- phase B: density weights
+      if (fits) {
+        for (int k0 = 0; k0 < nl; k0 += 32) {
+          const int k = k0 + lane;
+          const bool valid = k < nl;
+          int t = s, dx = 0, dy = 0, dz = 0;
+          if (valid) read_entry(L[k], t, dx, dy, dz);
+          test(valid, t, dx, dy, dz, valid ? __ldg(d.posf + t) : pi, true);
+        }
+      } else {
+#pragma unroll 1
+        for (int g = 0; g < nseg; g++) {
+          const int tb = S.tb[g], te = S.te[g];
+          if (tb >= te) continue;
+          const int code = S.code[g];
+          int b[2 * REACH];
+#pragma unroll
+          for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+          const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+          for (int t0 = tb; t0 < te; t0 += 32) {
+            const int t = t0 + lane;
+            const bool valid = t < te && t != s;
+            test(valid, valid ? t : s, fx0 + frame_step<REACH>(t, b), dy, dz,
+                 valid ? __ldg(d.posf + t) : pi, false);
+          }
         }
       }
     }
     __syncwarp();
+    if (fits) {  // list out for pass 2, coalesced
+      uint32_t* out = d.nbl + (size_t)s * kNbrCap;
+      for (int k = lane; k < nl; k += 32) out[k] = L[k];
+    }
     unsigned long long a0 = q0, a1 = q1, a2 = q2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -307,7 +343,92 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
         d.dqz[s] = (long long)a2;
       }
     }
+    __syncwarp();
   }
+}
+
+// The kept lists (rebuild steps only): one warp per particle sweeps the
+// neighbour segments of its cell like pass 1 and lists every candidate
+// closer than 1 + skin (FP32, with a margin: the list only has to hold every
+// pair that can come within the cutoff before the next rebuild). Also records
+// each slot's delta_sumr for the displacement test.
+template <int REACH>
+__global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
+  __shared__ SegTable seg[kWarps];
+  __shared__ uint32_t lst[kWarps][kVerletCap];
+  if (!d.vdev->rebuild) return;
+  const int r = d.blk_rep[blockIdx.x];
+  const RepDev* R = d.reps + r;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SegTable& S = seg[wid];
+  uint32_t* L = lst[wid];
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
+  const float rv2 = d.vdev->rv2;
+  const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
+  constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  int cached = -1;
+  for (int s = s0; s < s_end; s++) {
+    const int cell = (int)d.scell[s];
+    if (cell != cached) {
+      int cx, cy, cz;
+      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+      __syncwarp();
+      build_segments(S, d, R, cx, cy, cz, lane);
+      __syncwarp();
+      cached = cell;
+    }
+    const float4 pi = d.posf[s];
+    int nl = 0;
+#pragma unroll 1
+    for (int g = 0; g < nseg; g++) {
+      const int tb = S.tb[g], te = S.te[g];
+      if (tb >= te) continue;
+      const int code = S.code[g];
+      int b[2 * REACH];
+#pragma unroll
+      for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+      const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
+      for (int t0 = tb; t0 < te; t0 += 32) {
+        const int t = t0 + lane;
+        bool in = false;
+        int ddx = 0;
+        if (t < te && t != s) {
+          const float4 pj = __ldg(d.posf + t);
+          ddx = frame_step<REACH>(t, b);
+          const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
+                      ez = bz - pj.z;
+          in = ex * ex + ey * ey + ez * ez < rv2;
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, in);
+        if (in) {
+          const int pos = nl + __popc(mask & lt_mask);
+          if (pos < kVerletCap) L[pos] = make_entry(t, fx0 + ddx, dy, dz);
+        }
+        nl += __popc(mask);
+      }
+    }
+    __syncwarp();
+    const bool fits = nl <= kVerletCap;
+    if (fits) {
+      uint32_t* out = d.vl + (size_t)s * kVerletCap;
+      for (int k = lane; k < nl; k += 32) out[k] = L[k];
+    }
+    if (lane == 0) {
+      d.vn[s] = fits ? (uint16_t)nl : (uint16_t)kNbrFallback;
+      const uint32_t i = d.perm[s];
+      d.drx[s] = d.dsx[i];
+      d.dry[s] = d.dsy[i];
+      d.drz[s] = d.dsz[i];
+    }
+    __syncwarp();
+  }
+}
+
+void launch_verlet_build(const DevState& d, int nblk, cudaStream_t st) {
+  if (nblk > 0) k_verlet_build<1><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // Visits every neighbour cell within the stencil of the given reach
@@ -379,14 +500,17 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   }
 }
 
-void launch_density(const DevState& d, int nblk, bool fp64, int reach, cudaStream_t st) {
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
+                    cudaStream_t st) {
   if (nblk == 0) return;
   if (fp64)
     k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
+  else if (verlet)
+    k_density_f32<1, true><<<nblk, kRowBlock, 0, st>>>(d);
   else if (reach == 2)
-    k_density_f32<2><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<2, false><<<nblk, kRowBlock, 0, st>>>(d);
   else
-    k_density_f32<1><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<1, false><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // ------------------------------------------------------------- pass 2
@@ -512,16 +636,14 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
     I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
     const uint32_t cnt = d.nbn[s];
     if (cnt != kNbrFallback) {
-      const uint16_t* list = d.nbl + (size_t)s * kNbrCap;
+      const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
       uint32_t e_next = lane < (int)cnt ? list[lane] : 0u;  // one round ahead
       for (int k = lane; k < (int)cnt; k += 32) {
         const uint32_t e = e_next;
         if (k + 32 < (int)cnt) e_next = list[k + 32];
-        const int g = (int)(e & 63u);
-        const int code = S.code[g];
-        const int t = S.tb[g] + (int)(e >> 8);
-        eval_pair<PRESS>(d, R, T, I, t, (code & 7) - 4 + (int)((e >> 6) & 3u),
-                         ((code >> 3) & 7) - 4, ((code >> 6) & 7) - 4);
+        int t, dx, dy, dz;
+        read_entry(e, t, dx, dy, dz);
+        eval_pair<PRESS>(d, R, T, I, t, dx, dy, dz);
       }
     } else {
       int qn = 0;
@@ -549,8 +671,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
             near = fabsf(dr2 - 1.0f) <= kGuard;
           }
           if (__any_sync(0xffffffffu, near) && near) {
-            const PairCode pc = unpack_code(pack_code(dx, code));
-            in = exact_dr2(d, R, d.perm[s], d.perm[t], pc.sx, pc.sy, pc.sz) < 1.0;
+            in = exact_dr2(d, R, d.perm[s], d.perm[t]) < 1.0;
           }
           const uint32_t mask = __ballot_sync(0xffffffffu, in);
           if (in) {
@@ -744,7 +865,7 @@ __global__ void __launch_bounds__(kRowBlock) k_com(DevState d, double* cm, uint3
       if (dr2 >= rn2 + kGuard) continue;
       bool in_b = dr2 < rn2, in_l = dr2 < 1.0f;
       if (fabsf(dr2 - rn2) <= kGuard || fabsf(dr2 - 1.0f) <= kGuard || dr2 < 1.0e-10f) {
-        const double e2 = exact_dr2(d, R, i, d.perm[t], sx, sy, sz);
+        const double e2 = exact_dr2(d, R, i, d.perm[t]);
         in_b = e2 < rn2d && e2 != 0.0;
         in_l = in_b && e2 < 1.0;
       }

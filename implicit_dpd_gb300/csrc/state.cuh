@@ -41,7 +41,7 @@ struct DevState {
   uint32_t* scell;
   float4 *posf, *velf, *densf;
   float4* poslo;               // low-order parts of the cell-local position
-  uint16_t* nbl;               // [N * kNbrCap] in-range neighbours of pass 1 (sorted order)
+  uint32_t* nbl;               // [N * kNbrCap] in-range neighbours of pass 1 (sorted order)
   uint16_t* nbn;               // [N] list length, or 0xffff when the list overflowed
   long long *fqx, *fqy, *fqz;  // pair force, 2^-26 fixed point
   long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API only)
@@ -60,6 +60,23 @@ struct DevState {
   double* blk_part;  // [n_blocks * 3]
   double* rep_mean;  // [R * 3]
   int* err;          // device error word (0 = ok)
+  // ---- neighbour lists kept between rebuilds (null when the skin is 0)
+  uint32_t* vl;                // [N * kVerletCap] pairs within 1 + skin at the last rebuild
+  uint16_t* vn;                // [N] list length, or 0xffff when it did not fit
+  double *drx, *dry, *drz;     // delta_sumr at the last rebuild (sorted order)
+  struct VerletDev* vdev;
+};
+
+// The rebuild schedule of the kept lists: a rebuild when any particle moved
+// more than half the skin since the last one, or when forced (new layout,
+// new positions, particles added).
+struct VerletDev {
+  int rebuild;          // this step rebuilds the cells and lists
+  int force;            // the next step must rebuild
+  unsigned int maxd2;   // bits of the largest squared displacement (float, >= 0)
+  float thr2;           // (skin / 2)^2 less a margin
+  float rv2;            // build cutoff (1 + skin)^2 plus a margin
+  unsigned int rebuilds;
 };
 
 // Error codes written by kernels into DevState::err.
@@ -92,14 +109,23 @@ struct ChemDev {
 
 constexpr int kRowBlock = 128;  // rows per block of row-block launches
 constexpr int kNbrCap = 256;    // neighbour-list slots per particle
+constexpr int kVerletCap = 512; // kept-list slots per particle
 
 // kernels_cells.cu
 void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st);
 // start[ncell_tot] = reps[last_rep].row_off + reps[last_rep].n, read on the
 // device (the particle count can grow on the device).
-void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st);
+void launch_scan(const DevState& d, int ncell_tot, int last_rep, cudaStream_t st,
+                 const int* gate = nullptr);
+// Steps with kept lists: drift plus the largest displacement since the last
+// rebuild, the rebuild decision, and the binning of rebuild steps.
+void launch_drift_disp(const DevState& d, int nblk, cudaStream_t st);
+void launch_vl_decide(const DevState& d, cudaStream_t st);
+void launch_bin_gated(const DevState& d, int nblk, cudaStream_t st);
+// gate (may be null): device flag; when 0 the sort is skipped and the pack
+// keeps each slot's cell of the last rebuild.
 void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
-                              cudaStream_t st);
+                              cudaStream_t st, const int* gate = nullptr);
 void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol,
                     cudaStream_t st);
 void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
@@ -121,8 +147,12 @@ void set_library_error(const char* msg);
 // kernels_pairs.cu
 struct PairTuning {
   int reach;       // 1: cells of the cutoff, 27-cell stencil; 2: half cells, 125-cell stencil
+  float skin;      // > 0: lists of pairs within 1 + skin kept until a rebuild (reach 1)
 };
-void launch_density(const DevState& d, int nblk, bool fp64, int reach, cudaStream_t st);
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
+                    cudaStream_t st);
+// The kept lists of every particle (when this step rebuilds).
+void launch_verlet_build(const DevState& d, int nblk, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);

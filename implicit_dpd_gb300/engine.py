@@ -313,13 +313,25 @@ class Engine:
                                             C.cast(ptrs, C.c_void_p)), "retrieve_walks")
         return out
 
-    def set_tuning(self, reach):
-        self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach))), "set_tuning")
+    def set_tuning(self, reach, skin=None):
+        """reach 1 or 2; skin > 0 keeps the neighbour lists between rebuilds
+        (None: keep the current skin)."""
+        if skin is None:
+            cur = IdpdTuning()
+            self._ck(self.L.idpd_get_tuning(self.h, C.byref(cur)), "get_tuning")
+            skin = cur.skin
+        self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach, skin=skin))),
+                 "set_tuning")
 
     def get_tuning(self):
         t = IdpdTuning()
         self._ck(self.L.idpd_get_tuning(self.h, C.byref(t)), "get_tuning")
         return t.reach
+
+    def get_skin(self):
+        t = IdpdTuning()
+        self._ck(self.L.idpd_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t.skin
 
     def num_particles(self, replica=0):
         n = C.c_int32()

@@ -340,11 +340,17 @@ int idpd_write_xyz(const char* path, int32_t append, uint32_t time, int32_t n, c
                    const uint32_t* unit);
 
 /* ---- tuning --------------------------------------------------------------- */
-/* Launch and cell-grid shape of the pair passes. Every choice gives the same
+/* Launch and cell-grid shape of the pair passes. Every reach gives the same
  * results bit for bit (all pair sums are fixed point); only speed changes. */
 typedef struct idpd_tuning {
   int32_t reach;        /* 1: cells >= rc, 27-cell stencil; 2: cells >= rc/2, 125 cells */
-  int32_t reserved[7];
+  float skin;           /* > 0: keep each particle's list of pairs within rc + skin and
+                           rebuild cells and lists only when some particle has moved
+                           more than skin / 2 (cells >= rc + skin, reach 1; every box
+                           side >= 3 (rc + skin)). Pair sets stay exact; sums differ
+                           from skin 0 only by FP32 rounding of the cell-local
+                           coordinates. 0: cells and lists every step. */
+  int32_t reserved[6];
 } idpd_tuning;
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t);
 int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t);

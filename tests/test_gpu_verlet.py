@@ -1,0 +1,75 @@
+"""Kept neighbour lists (idpd_tuning.skin > 0): the engine rebuilds cells and
+lists only when a particle has moved more than half the skin. Every step
+must still see exactly the reference's pair set, so each step is compared
+with one oracle step from the engine's own state (drift bit-exact, forces
+within 1e-5), across rebuild and non-rebuild steps, storage reorders and
+periodic wraps."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from helpers import FORCE_TOL, mdpd_params, mixed_system, rel_force_err
+from implicit_dpd_gb300.engine import Engine, EngineError
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(p, st, n_amp, skin, sort_period=0):
+    e = Engine(sort_period=sort_period)
+    e.set_params(p)
+    e.upload(st)
+    e.build_topology(n_amp, [0, 3])
+    e.set_tuning(1, skin)
+    return e
+
+
+def _oracle_step(p, s0, n_amp, time):
+    ref = {k: s0[k].copy() for k in ("pos", "vel", "acc", "id", "prop")}
+    ref["topol"], ref["cf_bend"] = O.build_topology(s0["amp_id"], s0["unit"], n_amp, [0, 3], p.cf_b,
+                                                    p.cf_b_rigid)
+    po = type(p).from_buffer_copy(p)
+    po.time = time
+    O.md_step(po, ref, nthreads=4)
+    return ref
+
+
+@pytest.mark.parametrize("skin,sort_period", [(0.3, 0), (0.3, 7), (0.15, 5)])
+def test_kept_lists_give_the_reference_step(skin, sort_period):
+    box, st, n_amp = mixed_system(seed=9)
+    p = mdpd_params(box, time=60)
+    e = _engine(p, st, n_amp, skin, sort_period)
+    assert abs(e.get_skin() - skin) < 1e-7
+    done = 0
+    for target in (0, 1, 12, 45):
+        e.step(target - done)
+        done = target
+        s0 = e.download()
+        t0 = e.get_params().time
+        e.step(1)
+        done += 1
+        s1 = e.download()
+        ref = _oracle_step(p, s0, n_amp, t0)
+        assert np.array_equal(s1["pos"], ref["pos"]), target
+        assert rel_force_err(s1["acc"], ref["acc"])[0] < FORCE_TOL, target
+        f_rms = np.sqrt((ref["acc"] ** 2).sum(1).mean())
+        assert np.abs(s1["vel"] - ref["vel"]).max() < 0.5 * p.dt * FORCE_TOL * f_rms + 1e-12
+
+
+def test_kept_lists_follow_the_plain_trajectory():
+    box, st, n_amp = mixed_system(seed=2)
+    p = mdpd_params(box, time=5)
+    out = []
+    for skin in (0.0, 0.3):
+        e = _engine(p, st, n_amp, skin)
+        e.step(40)
+        out.append(e.download())
+    assert np.abs(out[0]["pos"] - out[1]["pos"]).max() < 1e-6
+    assert rel_force_err(out[1]["acc"], out[0]["acc"])[1] < 1e-4
+
+
+def test_skin_needs_room_in_the_box():
+    box, st, n_amp = mixed_system(box=(9.0, 10.0, 11.0))
+    e = Engine()
+    e.set_params(mdpd_params(box))
+    with pytest.raises(EngineError, match="skin"):
+        e.set_tuning(1, 2.5)
