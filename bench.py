@@ -51,6 +51,9 @@ PAIR_KERNELS = {
 STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
 KERNELS_PER_STEP = 14          # drift_bin, scan x3, scatter, cell_sort, pack,
                                # density, force, bonded_kick, cmdrift x3, time
+KERNELS_PER_KEPT_STEP = 17     # drift_disp, rebuild decision, gated bin, gated scan x3,
+                               # gated scatter / cell_sort / pack, gated list build,
+                               # density, force, bonded_kick, cmdrift x3, time
 KERNELS_PER_REORDER = 4        # gather, topology, identity, loc
 
 
@@ -439,11 +442,13 @@ def run_engine(args, rank, world, local_rank):
     e.step(max(args.warmup, 3))
     dist.barrier()
     e.sync()
+    rb0 = e.list_rebuilds()
     clk = Clocks(local_rank)
     clk.start()
     e.step(args.steps)  # CUDA events around the steps on the engine's stream
     ms = e.last_step_ms()
     clocks = clk.stop()
+    rebuilds = e.list_rebuilds() - rb0
     dist.barrier()
     ms_max = dist.max(ms)
     value = n * args.steps * world / (ms_max * 1e-3)
@@ -509,11 +514,13 @@ def run_engine(args, rank, world, local_rank):
            "data": "synthetic", "config": dict(workload_desc(n, n_amp, box, layers), equilibration_steps=args.equil,
                                                equilibration_s=t_eq, tuning=reach,
                                                autotune_ms_per_step=tune_ms,
+                                               list_rebuilds_in_timed_steps=rebuilds,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
            "batched_replicas": batched,
-           "gpu_launches": args.steps * KERNELS_PER_STEP + n_reorders * KERNELS_PER_REORDER,
+           "gpu_launches": args.steps * (KERNELS_PER_KEPT_STEP if reach["skin"] > 0 else KERNELS_PER_STEP)
+                           + n_reorders * KERNELS_PER_REORDER,
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -114,9 +114,8 @@ struct Saru {
 
 // Normal deviate of Saru::nrml() (saruprng.hpp:442-445) in FP32:
 // sqrt(-2 ln u1) cos(2 pi u2) with u = (2 (draw >> 1) + 1) / 2^32.
-// -ln u1 is taken from the exact complement 1 - u1 through log1p when u1 >=
-// 1/2, and the cosine argument is folded to (0, 1) in integers, so neither
-// factor loses relative accuracy at the ends of the interval.
+// -ln u1 is taken from the exact complement 1 - u1 when u1 >= 1/2, so it
+// keeps its relative accuracy as u1 -> 1.
 //
 // Both factors are evaluated without branches (lanes of a warp take
 // different ends of the interval):
@@ -125,9 +124,10 @@ struct Saru {
 //  * u1 >= 1/2: c = 1 - u1 comes exactly from the integer complement and
 //    -ln(1 - c) = 2 atanh(z), z = c / (2 - c) <= 1/3, from its Taylor series
 //    z + z^3/3 + ... + z^15/15 (truncation below 1e-8 relative);
-//  * cos(pi x): x is folded in integers to y in [0, 1/2] with a sign, then
-//    cos(pi y) for y <= 1/4 or sin(pi (1/2 - y)) from Taylor polynomials of
-//    degree 10 / 9 in pi y <= pi/4 (truncation below 2e-9).
+//  * cos(2 pi u2) = cos(2 pi (u2 - 1)): the draw read as a signed integer
+//    gives the argument in [-pi, pi), where the hardware cosine's absolute
+//    error is below 2^-21.4 (the deviate's error stays below 2.4e-6 for the
+//    largest radius, sqrt(2 ln 2^32) = 6.66).
 __device__ __forceinline__ float saru_nrml_f32(Saru& s) {
   const uint32_t m1 = s.next() | 1u;  // 2 (draw >> 1) + 1 = u1 * 2^32
   const uint32_t m2 = s.next() | 1u;  // u2 * 2^32
@@ -146,27 +146,8 @@ __device__ __forceinline__ float saru_nrml_f32(Saru& s) {
   p = fmaf(p, z2, 1.0f);
   const float lb = 2.0f * z * p;
   const float nlog = m1 < 0x80000000u ? la : lb;
-  // cos(2 pi u2) = cos(pi x), x = m2 / 2^31 in (0, 2)
-  uint32_t n = m2 > 0x80000000u ? 0u - m2 : m2;         // x -> 2 - x: x in (0, 1]
-  const float sgn = n > 0x40000000u ? -1.0f : 1.0f;     // cos(pi x) = -cos(pi (1 - x))
-  n = n > 0x40000000u ? 0x80000000u - n : n;            // y = n / 2^31 in [0, 1/2]
-  const bool use_cos = n <= 0x20000000u;                // y <= 1/4
-  const uint32_t a = use_cos ? n : 0x40000000u - n;     // pi y or pi (1/2 - y), <= pi/4
-  const float t = __uint2float_rn(a) * (3.14159265358979323846f * 4.6566128730773926e-10f);
-  const float t2 = t * t;
-  float pc = -1.0f / 3628800.0f;
-  pc = fmaf(pc, t2, 1.0f / 40320.0f);
-  pc = fmaf(pc, t2, -1.0f / 720.0f);
-  pc = fmaf(pc, t2, 1.0f / 24.0f);
-  pc = fmaf(pc, t2, -0.5f);
-  pc = fmaf(pc, t2, 1.0f);
-  float ps = 1.0f / 362880.0f;
-  ps = fmaf(ps, t2, -1.0f / 5040.0f);
-  ps = fmaf(ps, t2, 1.0f / 120.0f);
-  ps = fmaf(ps, t2, -1.0f / 6.0f);
-  ps = fmaf(ps, t2, 1.0f);
-  ps = ps * t;
-  const float cs = sgn * (use_cos ? pc : ps);
+  // cos(2 pi u2) = cos(2 pi (u2 - 1)): the signed draw gives the argument in [-pi, pi)
+  const float cs = __cosf(__int2float_rn((int)m2) * (6.28318530717958647692f * two_m32));
   const float r2 = 2.0f * nlog;
   return r2 * rsqrtf(r2) * cs;  // nlog > 0 for every odd m1
 }
@@ -243,13 +224,21 @@ __device__ __forceinline__ float fix_to_float(long long q, float unscale) {
 // mantissa of 1.5 * 2^23 + v 2^5 holds round(v 2^5) (hi); the remainder
 // v - hi 2^-5 is exact and |.| <= 2^-6, so a second rounding gives the low
 // 21 bits. Larger |v| take the bit-level path. Ties round to even.
-__device__ __forceinline__ long long fix_force(float v) {
-  if (!(fabsf(v) < 65536.0f)) return fix_from_float(v, kForceBits);
+// round(v * 2^26) = hi * 2^21 + lo for |v| < 65536: hi = round(v * 32)
+// (|hi| <= 2^21) and lo = round((v - hi / 32) * 2^26) (|lo| <= 2^20), both
+// read from the mantissa of 1.5 * 2^23 + x.
+__device__ __forceinline__ void fix_force_parts(float v, int& hi, int& lo) {
   const float magic = 12582912.0f;  // 1.5 * 2^23
   const float a = fmaf(v, 32.0f, magic);
-  const int hi = __float_as_int(a) - __float_as_int(magic);
+  hi = __float_as_int(a) - __float_as_int(magic);
   const float r = fmaf(-(a - magic), 0.03125f, v);
-  const int lo = __float_as_int(fmaf(r, 67108864.0f, magic)) - __float_as_int(magic);
+  lo = __float_as_int(fmaf(r, 67108864.0f, magic)) - __float_as_int(magic);
+}
+
+__device__ __forceinline__ long long fix_force(float v) {
+  if (!(fabsf(v) < 65536.0f)) return fix_from_float(v, kForceBits);
+  int hi, lo;
+  fix_force_parts(v, hi, lo);
   return ((long long)hi << 21) + (long long)lo;
 }
 

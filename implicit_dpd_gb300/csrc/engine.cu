@@ -1267,6 +1267,18 @@ int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t) {
   return IDPD_OK;
 }
 
+int idpd_list_rebuilds(idpd_handle* h, uint64_t* rebuilds) {
+  if (!h || !rebuilds) return IDPD_ERR_INVALID_ARG;
+  *rebuilds = 0;
+  if (!h->d.vdev) return IDPD_OK;
+  cudaSetDevice(h->device);
+  unsigned int n = 0;
+  CK(cudaMemcpyAsync(&n, &h->d.vdev->rebuilds, sizeof(n), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  *rebuilds = n;
+  return check_device_error(h);
+}
+
 int idpd_last_step_ms(const idpd_handle* h, float* ms) {
   if (!h || !ms) return IDPD_ERR_INVALID_ARG;
   *ms = h->last_ms;
@@ -1280,10 +1292,10 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   int rc = commit(h);
   if (rc) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
-  std::vector<cudaEvent_t> ev(9);
+  std::vector<cudaEvent_t> ev(10);
   for (auto& e : ev) CK(cudaEventCreate(&e));
-  const char* nm[8] = {"drift_bin", "scan", "scatter_sort_pack", "density", "force",
-                       "bonded_kick", "cmdrift", "time"};
+  const char* nm[9] = {"drift_bin", "scan", "scatter_sort_pack", "list_build", "density",
+                       "force", "bonded_kick", "cmdrift", "time"};
   int rc2 = ensure_verlet_ready(h);
   if (rc2) return rc2;
   DevState d = h->d;
@@ -1302,22 +1314,23 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
-  if (verlet) launch_verlet_build(d, h->nblk, h->st);
   CK(cudaEventRecord(ev[3], h->st));
-  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
+  if (verlet) launch_verlet_build(d, h->nblk, h->st);
   CK(cudaEventRecord(ev[4], h->st));
-  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
+  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_bonded_kick(d, h->nblk, true, h->st);
+  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
   CK(cudaEventRecord(ev[6], h->st));
-  launch_cmdrift(d, h->nblk, h->R, false, h->st);
+  launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[7], h->st));
-  launch_time_advance(d, h->R, h->st);
+  launch_cmdrift(d, h->nblk, h->R, false, h->st);
   CK(cudaEventRecord(ev[8], h->st));
-  CK(cudaEventSynchronize(ev[8]));
+  launch_time_advance(d, h->R, h->st);
+  CK(cudaEventRecord(ev[9], h->st));
+  CK(cudaEventSynchronize(ev[9]));
   std::string all;
   int k = 0;
-  for (; k < 8 && k < max_k; k++) {
+  for (; k < 9 && k < max_k; k++) {
     CK(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
     all += nm[k];
     all += "\n";

@@ -544,20 +544,41 @@ __device__ __forceinline__ float near_cut_w(float4 pi, float4 li, float4 pj, flo
 
 // The particle of one warp in pass 2 and its fixed-point sums.
 struct PairI {
-  float4 pi, vi, di, li;
+  float4 pi, vi, di;
   uint32_t idi, pri, seed;
+  int row;  // the particle's row (its low position parts are read near the cutoff)
   int form;
   float csx, csy, csz;
   long long fx, fy, fz, px, py, pz;
 };
 
-// One pair term added to the particle's sums (the lane's share).
+// A lane's share of one fixed-point sum of pass 2 as the sums of the
+// fix_force_parts of its terms. A list gives a lane at most kNbrCap / 32
+// terms, so the parts' warp totals stay below 2^29 and reduce in 32 bits.
+struct FixSum {
+  int hi, lo;
+  __device__ __forceinline__ void add(float v, bool& range) {
+    range &= fabsf(v) < 65536.0f;  // else the particle is summed again in 64 bits
+    int h, l;
+    fix_force_parts(v, h, l);
+    hi += h;
+    lo += l;
+  }
+  __device__ __forceinline__ long long total() const {
+    return ((long long)__reduce_add_sync(0xffffffffu, hi) << 21) +
+           (long long)__reduce_add_sync(0xffffffffu, lo);
+  }
+};
+static_assert((kNbrCap / 32) * (1 << 21) < (1 << 26), "32-bit warp totals of the fixed-point parts");
+
+// The force and virial terms of one pair (the pair arithmetic of pass 2).
 template <bool PRESS>
-__device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, const PairTables& T,
-                                          PairI& I, int t, int dx, int dy, int dz) {
+__device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, const PairTables& T,
+                                           const PairI& I, int t, int dx, int dy, int dz,
+                                           float g[6]) {
   const float4 vj = __ldg(d.velf + t);
   const uint32_t idj = fbits(vj.w);
-  if (idj == I.idi) return;  // nbdf_calculator.hpp:84
+  if (idj == I.idi) return false;  // nbdf_calculator.hpp:84
   const float4 pj = __ldg(d.posf + t);
   const float4 dj = __ldg(d.densf + t);
   const float ex = (I.pi.x - (float)dx * I.csx) - pj.x;
@@ -568,18 +589,46 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
   const float dr = dr2 * inv_dr;
   float w = 1.0f - dr;
   if (dr2 > kNearCut2)  // admitted pairs have 1 - r >= 0 up to ~1e-13
-    w = fmaxf(near_cut_w(I.pi, I.li, pj, __ldg(d.poslo + t), dx, dy, dz, R, dr), 0.0f);
+    w = fmaxf(near_cut_w(I.pi, __ldg(d.poslo + I.row), pj, __ldg(d.poslo + t), dx, dy, dz, R, dr),
+              0.0f);
   const float a = pair_all_cf(T, R, I.form, I.pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, I.vi, vj,
                               I.di, dj, I.idi, idj, I.seed);
   if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
-  const float gx = a * ex, gy = a * ey, gz = a * ez;
-  I.fx += fix_force(gx);
-  I.fy += fix_force(gy);
-  I.fz += fix_force(gz);
+  g[0] = a * ex;
+  g[1] = a * ey;
+  g[2] = a * ez;
   if (PRESS) {
-    I.px += fix_force(gx * ex);
-    I.py += fix_force(gy * ey);
-    I.pz += fix_force(gz * ez);
+    g[3] = g[0] * ex;
+    g[4] = g[1] * ey;
+    g[5] = g[2] * ez;
+  }
+  return true;
+}
+
+// One pair term added to the particle's sums in 32-bit parts.
+template <bool PRESS>
+__device__ __forceinline__ void eval_pair_parts(const DevState& d, const RepDev* R,
+                                                const PairTables& T, const PairI& I, int t, int dx,
+                                                int dy, int dz, FixSum f[6], bool& range) {
+  float g[6];
+  if (!pair_terms<PRESS>(d, R, T, I, t, dx, dy, dz, g)) return;
+#pragma unroll
+  for (int c = 0; c < (PRESS ? 6 : 3); c++) f[c].add(g[c], range);
+}
+
+// One pair term added to the particle's sums (the lane's share).
+template <bool PRESS>
+__device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, const PairTables& T,
+                                          PairI& I, int t, int dx, int dy, int dz) {
+  float g[6];
+  if (!pair_terms<PRESS>(d, R, T, I, t, dx, dy, dz, g)) return;
+  I.fx += fix_force(g[0]);
+  I.fy += fix_force(g[1]);
+  I.fz += fix_force(g[2]);
+  if (PRESS) {
+    I.px += fix_force(g[3]);
+    I.py += fix_force(g[4]);
+    I.pz += fix_force(g[5]);
   }
 }
 
@@ -618,34 +667,67 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
   for (int s = s0; s < s_end; s++) {
-    const int cell = (int)d.scell[s];
-    if (cell != cached) {
-      int cx, cy, cz;
-      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
-      __syncwarp();
-      build_segments(S, d, R, cx, cy, cz, lane);
-      __syncwarp();
-      cached = cell;
-    }
     I.pi = d.posf[s];
     I.vi = d.velf[s];
     I.di = d.densf[s];
-    I.li = d.poslo[s];
+    I.row = s;
     I.idi = fbits(I.vi.w);
     I.pri = fbits(I.pi.w);
-    I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
     const uint32_t cnt = d.nbn[s];
-    if (cnt != kNbrFallback) {
-      const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
+    const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
+    if (cnt != kNbrFallback) {  // the list: sums in 32-bit parts
+      FixSum f[6];
+#pragma unroll
+      for (int c = 0; c < 6; c++) f[c].hi = f[c].lo = 0;
+      bool range = true;
       uint32_t e_next = lane < (int)cnt ? list[lane] : 0u;  // one round ahead
       for (int k = lane; k < (int)cnt; k += 32) {
         const uint32_t e = e_next;
         if (k + 32 < (int)cnt) e_next = list[k + 32];
         int t, dx, dy, dz;
         read_entry(e, t, dx, dy, dz);
+        eval_pair_parts<PRESS>(d, R, T, I, t, dx, dy, dz, f, range);
+      }
+      if (__all_sync(0xffffffffu, range)) {
+        const long long fx = f[0].total(), fy = f[1].total(), fz = f[2].total();
+        long long px = 0, py = 0, pz = 0;
+        if (PRESS) {
+          px = f[3].total();
+          py = f[4].total();
+          pz = f[5].total();
+        }
+        if (lane == 0) {
+          d.fqx[s] = fx;
+          d.fqy[s] = fy;
+          d.fqz[s] = fz;
+          if (PRESS) {
+            d.pqx[s] = px;
+            d.pqy[s] = py;
+            d.pqz[s] = pz;
+          }
+        }
+        continue;
+      }
+    }
+    // a term outside the 32-bit parts' range, or a list that did not fit:
+    // 64-bit sums
+    I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
+    if (cnt != kNbrFallback) {
+      for (int k = lane; k < (int)cnt; k += 32) {
+        int t, dx, dy, dz;
+        read_entry(list[k], t, dx, dy, dz);
         eval_pair<PRESS>(d, R, T, I, t, dx, dy, dz);
       }
     } else {
+      const int cell = (int)d.scell[s];
+      if (cell != cached) {  // the segments of the particle's cell (only this path walks cells)
+        int cx, cy, cz;
+        cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+        __syncwarp();
+        build_segments(S, d, R, cx, cy, cz, lane);
+        __syncwarp();
+        cached = cell;
+      }
       int qn = 0;
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {

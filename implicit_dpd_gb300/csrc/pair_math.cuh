@@ -49,6 +49,8 @@ __device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* 
 }
 
 // Pairs with dr^2 above this take w = 1 - dr from the compensated path.
-constexpr float kNearCut2 = 0.98f;
+// Below it w > 1e-3, and the ~2e-7 absolute FP32 error of w moves the
+// random-force weight sqrt(w) by less than 4e-6.
+constexpr float kNearCut2 = 0.998f;
 
 }  // namespace idpd

@@ -32,7 +32,7 @@ EXPORTS = [
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
     "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
-    "idpd_write_xyz",
+    "idpd_write_xyz", "idpd_list_rebuilds",
 ]
 
 # The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
@@ -87,6 +87,7 @@ def load(path=LIB_PATH):
     L.idpd_set_dynamics.argtypes = [H, C.c_int32, VP, VP, VP]
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
+    L.idpd_list_rebuilds.argtypes = [H, C.POINTER(C.c_uint64)]
     L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
     L.idpd_set_chem.argtypes = [H, C.c_int32, C.POINTER(IdpdChemConfig)]
     L.idpd_chem_event.argtypes = [H, C.POINTER(C.c_int32)]
@@ -322,6 +323,12 @@ class Engine:
             skin = cur.skin
         self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach, skin=skin))),
                  "set_tuning")
+
+    def list_rebuilds(self):
+        """Steps that rebuilt the cells and kept lists (0 with skin 0)."""
+        n = C.c_uint64()
+        self._ck(self.L.idpd_list_rebuilds(self.h, C.byref(n)), "list_rebuilds")
+        return n.value
 
     def get_tuning(self):
         t = IdpdTuning()

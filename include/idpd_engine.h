@@ -354,6 +354,9 @@ typedef struct idpd_tuning {
 } idpd_tuning;
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t);
 int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t);
+/* Steps that rebuilt the cells and the kept lists since the lists were last
+ * (re)allocated; 0 while the skin is 0. */
+int idpd_list_rebuilds(idpd_handle* h, uint64_t* rebuilds);
 
 /* ---- timing -------------------------------------------------------------- */
 /* Elapsed milliseconds of the last idpd_step call measured with CUDA events

@@ -137,6 +137,28 @@ def test_warren_form_matches_fp64_restatement():
     assert rel_force_err(e.download()["acc"], acc)[0] < FORCE_TOL
 
 
+@pytest.mark.parametrize("a", [-40.0, -3.0e5])
+def test_large_pair_terms_take_the_64bit_sums(a):
+    """Pass 2 sums each lane's terms in two 32-bit parts and redoes a particle
+    in 64-bit sums when one of its terms is beyond +-65536; A = -3e5 puts
+    most pairs there. Both the step kernel (no virial) and the fine-grained
+    force call (with virial) are compared with the oracle."""
+    box = np.array([8.0, 8.0, 8.0])
+    st = configs.liquid(box, 6.0, seed=5)
+    p = warren_params(box, a=a, time=11)
+    dens, cm, cnt, acc, press = oracle_forces(p, st)
+    e = engine_for(p, st)
+    e.density()
+    e.force()
+    got = e.download()
+    assert rel_force_err(got["acc"], acc)[0] < FORCE_TOL
+    aux = e.download_aux(press=True)
+    assert np.abs(aux["press"] - press).max() / np.abs(press).max() < 1e-4
+    s1, ref = _step_compare(p, st, 0, [], 0)
+    assert rel_force_err(s1["acc"], ref["acc"])[0] < FORCE_TOL
+    assert np.array_equal(s1["pos"], ref["pos"])
+
+
 def test_bonded_matches_oracle():
     box, st, n_amp = mixed_system(jitter=0.15)
     p = mdpd_params(box, cf_s=50.0, cf_b=10.0, cf_b_rigid=30.0)
