@@ -401,10 +401,10 @@ def pinned(shape):
     return t, t.numpy()
 
 
-TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.2), (1, 0.3), (1, 0.4)]
+TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2), (2, 0.3)]
 
 
-def autotune(e, steps=20):
+def autotune(e, steps=40):
     """Times each (cell reach, skin) on the current state over enough steps
     to include list rebuilds, and keeps the fastest. The reach does not change
     results; a skin changes them only by FP32 rounding (pair sets exact)."""

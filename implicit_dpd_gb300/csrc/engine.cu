@@ -177,8 +177,7 @@ int check_params(idpd_handle* h, const idpd_params* p) {
 // splits each frame cell into `reach` cells per axis. Positions are stored
 // relative to frame cells, so the search grid never changes a pair term.
 void fill_repdev(RepDev& R, const idpd_params& p, int reach, float skin) {
-  if (skin > 0.0f) reach = 1;  // kept lists use cells of the cutoff plus the skin
-  const double cut = 1.0 + (double)skin;
+  const double cut = 1.0 + (double)skin;  // frame cells: the cutoff plus the skin
   R.reach = reach;
   R.rshift = reach == 2 ? 1 : 0;
   for (int k = 0; k < 3; k++) {
@@ -603,6 +602,7 @@ int check_device_error(idpd_handle* h) {
     case kErrNonFinite: return fail(h, IDPD_ERR_NONFINITE, "non-finite pair force");
     case kErrComBox: return fail(h, IDPD_ERR_INVALID_ARG, "neighbour centre of mass needs >= 5 cells per axis (box >= 5)");
     case kErrChemCapacity: return fail(h, IDPD_ERR_CAPACITY, "reaction event exceeds the reserved molecules (idpd_chem_config.reserve_amp)");
+    case kErrDensPairs: return fail(h, IDPD_ERR_CAPACITY, "more than %d pairs within the cutoff of one particle", kDensPairsMax);
     default: return fail(h, IDPD_ERR_STATE, "device error code %d", e);
   }
 }
@@ -630,7 +630,7 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_bin_gated(d, h->nblk, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
-    launch_verlet_build(d, h->nblk, h->st);
+    launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   } else {
     launch_drift_bin(d, h->nblk, true, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st);
@@ -1315,7 +1315,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
   CK(cudaEventRecord(ev[3], h->st));
-  if (verlet) launch_verlet_build(d, h->nblk, h->st);
+  if (verlet) launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   CK(cudaEventRecord(ev[5], h->st));

@@ -225,8 +225,9 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
     const uint32_t nv = VERLET ? (uint32_t)d.vn[s] : kNbrFallback;
     bool fits = true;
     if (VERLET && nv != kNbrFallback) {
-      // ---- the particle's kept list: test, weight and list in one pass
+      // ---- the particle's kept list: test, weight and list out in one pass
       const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
+      uint32_t* out = d.nbl + (size_t)s * kNbrCap;
       uint32_t e_next = lane < (int)nv ? vl[lane] : 0u;  // one round ahead
       for (int k0 = 0; k0 < (int)nv; k0 += 32) {
         const int k = k0 + lane;
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
         const uint32_t mask = __ballot_sync(0xffffffffu, in1);
         if (in1) {
           const int pos = nl + __popc(mask & lt_mask);
-          if (pos < kNbrCap) L[pos] = e;
+          if (pos < kNbrCap) out[pos] = e;
         }
         nl += __popc(mask);
       }
@@ -302,6 +303,8 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
           test(valid, t, dx, dy, dz, valid ? __ldg(d.posf + t) : pi, true);
         }
       } else {
+        // a lane takes at most nseg + nl / 32 weights below 2^23 each
+        if (nl > kDensPairsMax && lane == 0) atomicCAS(d.err, 0, kErrDensPairs);
 #pragma unroll 1
         for (int g = 0; g < nseg; g++) {
           const int tb = S.tb[g], te = S.te[g];
@@ -321,16 +324,25 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
       }
     }
     __syncwarp();
-    if (fits) {  // list out for pass 2, coalesced
+    if (!VERLET && fits) {  // list out for pass 2, coalesced
       uint32_t* out = d.nbl + (size_t)s * kNbrCap;
       for (int k = lane; k < nl; k += 32) out[k] = L[k];
     }
-    unsigned long long a0 = q0, a1 = q1, a2 = q2;
+    // each weight is below 2^23, so up to 512 weighted pairs (every list:
+    // kept lists hold <= 512 candidates, pass-1 lists 256) total below 2^32
+    unsigned long long a0, a1, a2;
+    if (nl <= 512) {
+      a0 = __reduce_add_sync(0xffffffffu, q0);
+      a1 = __reduce_add_sync(0xffffffffu, q1);
+      a2 = __reduce_add_sync(0xffffffffu, q2);
+    } else {
+      a0 = q0, a1 = q1, a2 = q2;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
     }
     if (lane == 0) {
       const float u = R->dens_unscale_f;
@@ -427,8 +439,12 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   }
 }
 
-void launch_verlet_build(const DevState& d, int nblk, cudaStream_t st) {
-  if (nblk > 0) k_verlet_build<1><<<nblk, kRowBlock, 0, st>>>(d);
+void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st) {
+  if (nblk == 0) return;
+  if (reach == 2)
+    k_verlet_build<2><<<nblk, kRowBlock, 0, st>>>(d);
+  else
+    k_verlet_build<1><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // Visits every neighbour cell within the stencil of the given reach
@@ -505,6 +521,8 @@ void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verl
   if (nblk == 0) return;
   if (fp64)
     k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
+  else if (verlet && reach == 2)
+    k_density_f32<2, true><<<nblk, kRowBlock, 0, st>>>(d);
   else if (verlet)
     k_density_f32<1, true><<<nblk, kRowBlock, 0, st>>>(d);
   else if (reach == 2)

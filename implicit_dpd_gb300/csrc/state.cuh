@@ -81,7 +81,10 @@ struct VerletDev {
 
 // Error codes written by kernels into DevState::err.
 enum : int { kErrNone = 0, kErrCellOverflow = 1, kErrBadCell = 2, kErrListOverflow = 3,
-             kErrNonFinite = 4, kErrComBox = 5, kErrChemCapacity = 6 };
+             kErrNonFinite = 4, kErrComBox = 5, kErrChemCapacity = 6, kErrDensPairs = 7 };
+// Pairs within the cutoff of one particle that pass 1 can weigh (its lanes
+// keep 32-bit partial densities: (18 + kDensPairsMax / 32) * 2^23 < 2^32).
+constexpr int kDensPairsMax = 15000;
 
 // Device state of ChemManager (chemmanager.hpp:3-282) for replica 0 of a
 // one-replica handle: the MT19937 generator of PS::MT, the Parameter
@@ -152,7 +155,7 @@ struct PairTuning {
 void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
                     cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
-void launch_verlet_build(const DevState& d, int nblk, cudaStream_t st);
+void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);

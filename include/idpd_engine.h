@@ -346,7 +346,7 @@ typedef struct idpd_tuning {
   int32_t reach;        /* 1: cells >= rc, 27-cell stencil; 2: cells >= rc/2, 125 cells */
   float skin;           /* > 0: keep each particle's list of pairs within rc + skin and
                            rebuild cells and lists only when some particle has moved
-                           more than skin / 2 (cells >= rc + skin, reach 1; every box
+                           more than skin / 2 (cells >= (rc + skin) / reach; every box
                            side >= 3 (rc + skin)). Pair sets stay exact; sums differ
                            from skin 0 only by FP32 rounding of the cell-local
                            coordinates. 0: cells and lists every step. */

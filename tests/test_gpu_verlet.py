@@ -14,12 +14,12 @@ from implicit_dpd_gb300.engine import Engine, EngineError
 pytestmark = pytest.mark.gpu
 
 
-def _engine(p, st, n_amp, skin, sort_period=0):
+def _engine(p, st, n_amp, skin, sort_period=0, reach=1):
     e = Engine(sort_period=sort_period)
     e.set_params(p)
     e.upload(st)
     e.build_topology(n_amp, [0, 3])
-    e.set_tuning(1, skin)
+    e.set_tuning(reach, skin)
     return e
 
 
@@ -33,11 +33,12 @@ def _oracle_step(p, s0, n_amp, time):
     return ref
 
 
-@pytest.mark.parametrize("skin,sort_period", [(0.3, 0), (0.3, 7), (0.15, 5)])
-def test_kept_lists_give_the_reference_step(skin, sort_period):
+@pytest.mark.parametrize("skin,sort_period,reach", [(0.3, 0, 1), (0.3, 7, 1), (0.15, 5, 1),
+                                                    (0.3, 0, 2), (0.2, 5, 2)])
+def test_kept_lists_give_the_reference_step(skin, sort_period, reach):
     box, st, n_amp = mixed_system(seed=9)
     p = mdpd_params(box, time=60)
-    e = _engine(p, st, n_amp, skin, sort_period)
+    e = _engine(p, st, n_amp, skin, sort_period, reach)
     assert abs(e.get_skin() - skin) < 1e-7
     done = 0
     for target in (0, 1, 12, 45):
@@ -59,12 +60,16 @@ def test_kept_lists_follow_the_plain_trajectory():
     box, st, n_amp = mixed_system(seed=2)
     p = mdpd_params(box, time=5)
     out = []
-    for skin in (0.0, 0.3):
-        e = _engine(p, st, n_amp, skin)
+    for skin, reach in ((0.0, 1), (0.3, 1), (0.3, 2)):
+        e = _engine(p, st, n_amp, skin, reach=reach)
         e.step(40)
         out.append(e.download())
-    assert np.abs(out[0]["pos"] - out[1]["pos"]).max() < 1e-6
-    assert rel_force_err(out[1]["acc"], out[0]["acc"])[1] < 1e-4
+    for o in out[1:]:
+        assert np.abs(out[0]["pos"] - o["pos"]).max() < 1e-6
+        assert rel_force_err(o["acc"], out[0]["acc"])[1] < 1e-4
+    # the reach changes neither the pair sets nor the fixed-point sums
+    assert np.array_equal(out[1]["pos"], out[2]["pos"])
+    assert np.array_equal(out[1]["acc"], out[2]["acc"])
 
 
 def test_skin_needs_room_in_the_box():
