@@ -359,83 +359,105 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
   }
 }
 
-// The kept lists (rebuild steps only): one warp per particle sweeps the
-// neighbour segments of its cell like pass 1 and lists every candidate
-// closer than 1 + skin (FP32, with a margin: the list only has to hold every
-// pair that can come within the cutoff before the next rebuild). Also records
-// each slot's delta_sumr for the displacement test.
+// The kept lists (rebuild steps only). The particles of one cell share its
+// stencil of neighbour segments and, per candidate, the frame offset, so a
+// warp takes one cell at a time and up to 32 of its particles at once: each
+// lane loads one candidate, every particle of the batch is tested against
+// the 32 candidates (one ballot per particle), and each lane then appends
+// the candidates in range of its own particle to that particle's list. A
+// candidate is kept when closer than 1 + skin in FP32 (with a margin: the
+// list only has to hold every pair that can come within the cutoff before
+// the next rebuild). The warp of a 32-row chunk takes the cells whose first
+// row lies in the chunk. Also records each row's delta_sumr for the
+// displacement test.
 template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   __shared__ SegTable seg[kWarps];
-  __shared__ uint32_t lst[kWarps][kVerletCap];
+  __shared__ float4 bpos[kWarps][32];
+  __shared__ uint32_t ent[kWarps][32];
   if (!d.vdev->rebuild) return;
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
-  uint32_t* L = lst[wid];
+  float4* P = bpos[wid];
+  uint32_t* E = ent[wid];
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const float rv2 = d.vdev->rv2;
   const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
   constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  int cached = -1;
-  for (int s = s0; s < s_end; s++) {
-    const int cell = (int)d.scell[s];
-    if (cell != cached) {
-      int cx, cy, cz;
-      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+  bool first = false;
+  if (s0 + lane < s_end) first = d.cell_start[d.scell[s0 + lane]] == s0 + lane;
+  uint32_t starts = __ballot_sync(0xffffffffu, first);
+  while (starts) {
+    const int cs = s0 + __ffs(starts) - 1;
+    starts &= starts - 1;
+    const int cell = (int)d.scell[cs];
+    const int ce = d.cell_start[cell + 1];
+    int cx, cy, cz;
+    cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+    __syncwarp();
+    build_segments(S, d, R, cx, cy, cz, lane);
+    for (int b0 = cs; b0 < ce; b0 += 32) {
+      const int nb = min(32, ce - b0);
+      const int me = b0 + lane;  // the lane's particle (lane < nb)
       __syncwarp();
-      build_segments(S, d, R, cx, cy, cz, lane);
+      P[lane] = lane < nb ? d.posf[me] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       __syncwarp();
-      cached = cell;
-    }
-    const float4 pi = d.posf[s];
-    int nl = 0;
+      uint32_t* out = d.vl + (size_t)me * kVerletCap;
+      int cnt = 0;
 #pragma unroll 1
-    for (int g = 0; g < nseg; g++) {
-      const int tb = S.tb[g], te = S.te[g];
-      if (tb >= te) continue;
-      const int code = S.code[g];
-      int b[2 * REACH];
+      for (int g = 0; g < nseg; g++) {
+        const int tb = S.tb[g], te = S.te[g];
+        if (tb >= te) continue;
+        const int code = S.code[g];
+        int b[2 * REACH];
 #pragma unroll
-      for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
-      const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
-      const float by = pi.y - (float)dy * csy, bz = pi.z - (float)dz * csz;
-      for (int t0 = tb; t0 < te; t0 += 32) {
-        const int t = t0 + lane;
-        bool in = false;
-        int ddx = 0;
-        if (t < te && t != s) {
-          const float4 pj = __ldg(d.posf + t);
-          ddx = frame_step<REACH>(t, b);
-          const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
-                      ez = bz - pj.z;
-          in = ex * ex + ey * ey + ez * ez < rv2;
+        for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+        const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+        for (int t0 = tb; t0 < te; t0 += 32) {
+          const int t = t0 + lane;
+          // the candidate in the frame of the cell's particles (far away when absent)
+          float qx = 1.0e30f, qy = 0.0f, qz = 0.0f;
+          uint32_t e = 0;
+          if (t < te) {
+            const float4 pj = __ldg(d.posf + t);
+            const int fx = fx0 + frame_step<REACH>(t, b);
+            qx = fmaf((float)fx, csx, pj.x);
+            qy = fmaf((float)dy, csy, pj.y);
+            qz = fmaf((float)dz, csz, pj.z);
+            e = make_entry(t, fx, dy, dz);
+          }
+          __syncwarp();
+          E[lane] = e;
+          uint32_t mine = 0;  // candidates in range of the lane's particle
+#pragma unroll 4
+          for (int k = 0; k < nb; k++) {
+            const float4 pk = P[k];
+            const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
+            const uint32_t m = __ballot_sync(0xffffffffu, ex * ex + ey * ey + ez * ez < rv2);
+            mine = lane == k ? m : mine;
+          }
+          const unsigned self = (unsigned)(me - t0);  // the particle itself is no candidate
+          if (self < 32u && me < te) mine &= ~(1u << self);
+          __syncwarp();
+          while (mine) {
+            const int j = __ffs(mine) - 1;
+            mine &= mine - 1;
+            if (cnt < kVerletCap) out[cnt] = E[j];
+            cnt++;
+          }
         }
-        const uint32_t mask = __ballot_sync(0xffffffffu, in);
-        if (in) {
-          const int pos = nl + __popc(mask & lt_mask);
-          if (pos < kVerletCap) L[pos] = make_entry(t, fx0 + ddx, dy, dz);
-        }
-        nl += __popc(mask);
+      }
+      if (lane < nb) {
+        d.vn[me] = cnt <= kVerletCap ? (uint16_t)cnt : (uint16_t)kNbrFallback;
+        const uint32_t i = d.perm[me];
+        d.drx[me] = d.dsx[i];
+        d.dry[me] = d.dsy[i];
+        d.drz[me] = d.dsz[i];
       }
     }
-    __syncwarp();
-    const bool fits = nl <= kVerletCap;
-    if (fits) {
-      uint32_t* out = d.vl + (size_t)s * kVerletCap;
-      for (int k = lane; k < nl; k += 32) out[k] = L[k];
-    }
-    if (lane == 0) {
-      d.vn[s] = fits ? (uint16_t)nl : (uint16_t)kNbrFallback;
-      const uint32_t i = d.perm[s];
-      d.drx[s] = d.dsx[i];
-      d.dry[s] = d.dsy[i];
-      d.drz[s] = d.dsz[i];
-    }
-    __syncwarp();
   }
 }
 
