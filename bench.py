@@ -309,6 +309,42 @@ def run_reference(args, rank, world, budget_s=90.0):
     print(json.dumps(out), flush=True)
 
 
+def reaction_bench(tune, steps=100, equil=2000, device=0):
+    """The membrane with precursors: the stacked bilayers of the headline
+    workload plus single precursor beads at 10% of the bead count, uniform in
+    the box, each converted to a head bead with p = 1e-4 per step when a tail
+    bead lies within the cutoff (Saru draw keyed on (id, step, seed)).
+    Returns particle-steps/s with the conversion on, and the conversions."""
+    from implicit_dpd_gb300.abi import HYPHIL, HYPHOB, SOLVENT, precursor_threshold
+
+    st, n_amp, rp = workload()
+    box = np.asarray(BOX, np.float64)
+    n_pre = len(st["pos"]) // 10
+    pre = configs.liquid(box, n_pre / box.prod(), seed=777, prop=SOLVENT)
+    both = {k: np.concatenate([st[k], pre[k]]) for k in ("pos", "vel", "acc", "prop", "amp_id",
+                                                          "unit")}
+    n = len(both["pos"])
+    both["id"] = np.arange(n, dtype=np.uint32)
+    e = make_engine(both, n_amp, rp, device=device)
+    e.set_tuning(tune["reach"], tune["skin"])
+    e.step(equil)
+    e.set_precursor(SOLVENT, HYPHOB, HYPHIL, precursor_threshold(1e-4), 2024)
+    e.step(3)
+    e.sync()
+    c0 = e.precursor_count()
+    e.step(steps)
+    ms = e.last_step_ms()
+    conv = e.precursor_count() - c0
+    e.close()
+    return {"workload": "membrane_precursor_1m", "n_particles": int(n), "n_precursor": int(len(pre["pos"])),
+            "steps": steps, "equilibration_steps": equil, "value": n * steps / (ms * 1e-3),
+            "unit": "particle-steps/s", "ms_per_step": ms / steps, "conversions": int(conv),
+            "tuning": tune,
+            "description": "the membrane_1m bilayers plus 10% single precursor beads (uniform), "
+                           "converted to heads with p = 1e-4 per step within the cutoff of a "
+                           "tail bead (Saru(id, step, seed) draw, bit-exact decisions)"}
+
+
 def replicas_bench(steps=20, n_rep=256, device=0):
     """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
     A in [-50, -30], B = 25, densities 5-7): all replicas in one handle,
@@ -506,6 +542,7 @@ def run_engine(args, rank, world, local_rank):
                "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state per step"}
 
     batched = replicas_bench(device=local_rank) if not args.no_replicas else None
+    reaction = reaction_bench(reach, device=local_rank) if not args.no_reaction else None
     cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
     n_reorders = args.steps // 100
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -518,7 +555,7 @@ def run_engine(args, rank, world, local_rank):
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
-           "batched_replicas": batched,
+           "batched_replicas": batched, "reaction": reaction,
            "gpu_launches": args.steps * (KERNELS_PER_KEPT_STEP if reach["skin"] > 0 else KERNELS_PER_STEP)
                            + n_reorders * KERNELS_PER_REORDER,
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
@@ -540,6 +577,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-replicas", action="store_true")
+    ap.add_argument("--no-reaction", action="store_true",
+                    help="skip the membrane-with-precursor line")
     ap.add_argument("--box", type=float, nargs=3, default=list(BOX),
                     help="periodic box of the stacked-bilayer workload")
     ap.add_argument("--layers", type=int, default=N_LAYERS, help="bilayers stacked along z")

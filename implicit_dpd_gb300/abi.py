@@ -147,6 +147,17 @@ class IdpdTuning(C.Structure):
     _fields_ = [("reach", C.c_int32), ("skin", C.c_float), ("reserved", C.c_int32 * 6)]
 
 
+class IdpdPrecursor(C.Structure):
+    _fields_ = [("prop_from", C.c_uint32), ("prop_near", C.c_uint32), ("prop_to", C.c_uint32),
+                ("threshold", C.c_uint32), ("seed", C.c_uint32), ("enabled", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
+
+
+def precursor_threshold(p):
+    """The u32 threshold of a conversion probability p per step: floor(p 2^32)."""
+    return min(int(p * 4294967296.0), 0xFFFFFFFF)
+
+
 def params_to_dict(p):
     import numpy as np
 

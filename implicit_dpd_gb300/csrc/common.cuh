@@ -67,6 +67,9 @@ struct RepDev {
   float dens_prescale;    // 2^-k with every density weight * 2^-k <= 1
   float dens_unscale_f;   // 2^(k - 23): one unit of the density fixed point
   double dens_unscale;
+  // precursor conversion (idpd_precursor)
+  int prec_on;
+  uint32_t prec_from, prec_near, prec_to, prec_thr, prec_seed;
 };
 
 // FP64 coefficient tables of a replica (plain FP64 kernels).

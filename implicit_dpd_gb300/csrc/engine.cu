@@ -71,6 +71,10 @@ struct idpd_handle {
   std::string err;
   // chemistry (replica 0 of a one-replica handle)
   bool chem_on = false;
+  // precursor conversion, per replica
+  std::vector<idpd_precursor> prec;
+  bool prec_any = false;
+  unsigned long long* prec_dev = nullptr;  // [R] conversions
   idpd_chem_config chem_cfg{};
   ChemDev* chem = nullptr;        // device, kept across re-layouts (MT state)
   ChemBuffers chem_buf{};         // scratch, sized with the layout
@@ -215,6 +219,18 @@ void fill_repdev(RepDev& R, const idpd_params& p, int reach, float skin) {
   R.dens_prescale = (float)std::ldexp(1.0, -k);
   R.dens_unscale = std::ldexp(1.0, k - 23);
   R.dens_unscale_f = (float)R.dens_unscale;
+}
+
+// fill_repdev plus the replica's precursor conversion.
+void fill_rep(const idpd_handle* h, int r, RepDev& R) {
+  fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
+  const idpd_precursor& q = h->prec[r];
+  R.prec_on = q.enabled ? 1 : 0;
+  R.prec_from = q.prop_from;
+  R.prec_near = q.prop_near;
+  R.prec_to = q.prop_to;
+  R.prec_thr = q.threshold;
+  R.prec_seed = q.seed;
 }
 
 // Allocates (or grows) every device array for the current layout.
@@ -428,7 +444,7 @@ int commit(idpd_handle* h) {
     std::vector<int> blk_rep, blk_row;
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
-      fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
+      fill_rep(h, r, R);
       // a reaction appends molecules on the device: room for them after the rows
       const int extra_amp = (h->chem_on && r == 0) ? h->chem_cfg.reserve_amp : 0;
       R.row_off = row;
@@ -524,7 +540,7 @@ int commit(idpd_handle* h) {
     for (int r = 0; r < h->R; r++) {
       RepDev& R = h->reps_h[r];
       const RepDev keep = R;
-      fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
+      fill_rep(h, r, R);
       R.row_off = keep.row_off; R.n = keep.n; R.cell_off = keep.cell_off; R.blk_off = keep.blk_off;
       R.nblk = keep.nblk; R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
       if (R.ncell != keep.ncell) return fail(h, IDPD_ERR_STATE, "box change alters the cell grid; re-upload the state");
@@ -577,7 +593,7 @@ int retune_cells(idpd_handle* h) {
   for (int r = 0; r < h->R; r++) {
     RepDev& R = h->reps_h[r];
     const RepDev keep = R;
-    fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
+    fill_rep(h, r, R);
     R.row_off = keep.row_off; R.n = keep.n; R.blk_off = keep.blk_off; R.nblk = keep.nblk;
     R.n_amp = keep.n_amp; R.amp_off = keep.amp_off;
     R.cell_off = cell;
@@ -638,6 +654,10 @@ void enqueue_step(idpd_handle* h, bool observe) {
   }
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   launch_force(d, h->nblk, fp64, observe, h->tune, h->st);
+  if (h->prec_any) {
+    d.prec_count = h->prec_dev;
+    launch_precursor(d, h->nblk, !fp64, h->st);
+  }
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
   launch_cmdrift(d, h->nblk, h->R, false, h->st);
@@ -777,6 +797,7 @@ int idpd_create(const idpd_config* cfg, idpd_handle** out) {
   h->R = cfg->n_replicas;
   h->params.assign(h->R, idpd_params{});
   h->params_set.assign(h->R, 0);
+  h->prec.assign(h->R, idpd_precursor{});
   h->staged.assign(h->R, Staged{});
   h->n.assign(h->R, 0);
   h->n_amp.assign(h->R, 0);
@@ -799,6 +820,7 @@ int idpd_destroy(idpd_handle* h) {
   if (h->walks) walk_destroy(h->walks);
   if (h->obs_rec) cudaFree(h->obs_rec);
   if (h->obs_count) cudaFree(h->obs_count);
+  if (h->prec_dev) cudaFree(h->prec_dev);
   if (h->chem_flag_host) cudaFreeHost(h->chem_flag_host);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1540,6 +1562,42 @@ int idpd_retrieve_walks(idpd_handle* h, int32_t kind, int32_t tag, int32_t n_wal
   std::string err;
   const int rc = walk_retrieve(h->walks, kind, tag, n_walk, ni, result, err);
   if (rc) return fail(h, rc, "retrieve_walks: %s", err.c_str());
+  return IDPD_OK;
+}
+
+int idpd_set_precursor(idpd_handle* h, int32_t r, const idpd_precursor* cfg) {
+  if (!h) return fail(h, IDPD_ERR_INVALID_ARG, "null handle");
+  if (r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", r);
+  idpd_precursor q{};
+  if (cfg && cfg->enabled) {
+    if (cfg->prop_from >= IDPD_PROP_NUM || cfg->prop_near >= IDPD_PROP_NUM ||
+        cfg->prop_to >= IDPD_PROP_NUM)
+      return fail(h, IDPD_ERR_INVALID_ARG, "properties must be below %d", IDPD_PROP_NUM);
+    q = *cfg;
+    q.enabled = 1;
+  }
+  cudaSetDevice(h->device);
+  if (!h->prec_dev) CK(cudaMalloc((void**)&h->prec_dev, sizeof(unsigned long long) * h->R));
+  if (!h->prec_any) CK(cudaMemsetAsync(h->prec_dev, 0, sizeof(unsigned long long) * h->R, h->st));
+  CK(cudaMemsetAsync(h->prec_dev + r, 0, sizeof(unsigned long long), h->st));
+  h->prec[r] = q;
+  h->prec_any = false;
+  for (const idpd_precursor& p : h->prec) h->prec_any = h->prec_any || p.enabled;
+  h->reps_dirty = true;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+int idpd_precursor_count(idpd_handle* h, int32_t r, uint64_t* conversions) {
+  if (!h || !conversions) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
+  if (r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", r);
+  *conversions = 0;
+  if (!h->prec_dev) return IDPD_OK;
+  cudaSetDevice(h->device);
+  unsigned long long c = 0;
+  CK(cudaMemcpyAsync(&c, h->prec_dev + r, sizeof(c), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  *conversions = c;
   return IDPD_OK;
 }
 

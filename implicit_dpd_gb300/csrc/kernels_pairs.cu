@@ -944,6 +944,54 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
   }
 }
 
+// ------------------------------------------- precursor conversion
+// idpd_precursor: one warp per 32-row chunk, a particle at a time. A
+// particle of prop_from looks for a particle of prop_near among its pairs
+// within the cutoff: the pass-1 list of the step, or (no list: FP64 arm,
+// list overflow) a sweep of the cells around it with the reference's FP64
+// distance. The draw is Saru(id, time, seed).u32() (saruprng.hpp:239-255,
+// 322-333); properties change in the FP64 rows, so the pair passes see them
+// from the next step's packing on.
+__global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int lists) {
+  const int r = d.blk_rep[blockIdx.x];
+  const RepDev* R = d.reps + r;
+  if (!R->prec_on) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
+  const uint32_t from = R->prec_from, near_prop = R->prec_near;
+  for (int s = s0; s < s_end; s++) {
+    if (fbits(d.posf[s].w) != from) continue;
+    bool near = false;
+    const uint32_t cnt = lists ? (uint32_t)d.nbn[s] : kNbrFallback;
+    if (cnt != kNbrFallback) {
+      const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
+      for (int k = lane; k < (int)cnt; k += 32)
+        near |= fbits(__ldg(d.posf + (list[k] & kRowMask)).w) == near_prop;
+    } else {
+      const uint32_t i = d.perm[s];
+      int cx, cy, cz;
+      cell_xyz((int)d.scell[s] - R->cell_off, R->nc, cx, cy, cz);
+      for_each_cell(R, R->reach, cx, cy, cz, [&](int c, int, int, int, int, int, int) {
+        for (int t = d.cell_start[c] + lane; t < d.cell_start[c + 1]; t += 32)
+          if (t != s && fbits(d.posf[t].w) == near_prop && exact_dr2(d, R, i, d.perm[t]) < 1.0)
+            near = true;
+      });
+    }
+    if (__any_sync(0xffffffffu, near) && lane == 0) {
+      Saru g(fbits(d.velf[s].w), d.rep_time[r], R->prec_seed);
+      if (g.next() < R->prec_thr) {
+        d.prop[d.perm[s]] = R->prec_to;
+        atomicAdd(d.prec_count + r, 1ull);
+      }
+    }
+  }
+}
+
+void launch_precursor(const DevState& d, int nblk, bool lists, cudaStream_t st) {
+  if (nblk > 0) k_precursor<<<nblk, kRowBlock, 0, st>>>(d, lists ? 1 : 0);
+}
+
 // -------------------------------------------- neighbour centre of mass
 // The hydrophilic / hydrophobic neighbour sums of pass 1
 // (nbdf_calculator.hpp:23-51) and FPDPD::copyFromForce (ptcl_class.hpp:53-57),

@@ -60,6 +60,7 @@ struct DevState {
   double* blk_part;  // [n_blocks * 3]
   double* rep_mean;  // [R * 3]
   int* err;          // device error word (0 = ok)
+  unsigned long long* prec_count;  // [R] precursor conversions per replica
   // ---- neighbour lists kept between rebuilds (null when the skin is 0)
   uint32_t* vl;                // [N * kVerletCap] pairs within 1 + skin at the last rebuild
   uint16_t* vn;                // [N] list length, or 0xffff when it did not fit
@@ -155,6 +156,9 @@ struct PairTuning {
 void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
                     cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
+// Precursor conversion after the force pass (lists: the step's pass-1 lists
+// are valid; else the cells are swept).
+void launch_precursor(const DevState& d, int nblk, bool lists, cudaStream_t st);
 void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
                   cudaStream_t st);

@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from .abi import (STATUS_NAMES, IdpdChemConfig, IdpdChemInfo, IdpdConfig, IdpdObservation,
-                  IdpdParams, IdpdRunFile, IdpdRunParam, IdpdTuning)
+                  IdpdParams, IdpdPrecursor, IdpdRunFile, IdpdRunParam, IdpdTuning)
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libidpd_engine.so")
@@ -32,7 +32,7 @@ EXPORTS = [
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
     "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
-    "idpd_write_xyz", "idpd_list_rebuilds",
+    "idpd_write_xyz", "idpd_list_rebuilds", "idpd_set_precursor", "idpd_precursor_count",
 ]
 
 # The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
@@ -88,6 +88,8 @@ def load(path=LIB_PATH):
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_list_rebuilds.argtypes = [H, C.POINTER(C.c_uint64)]
+    L.idpd_set_precursor.argtypes = [H, C.c_int32, C.POINTER(IdpdPrecursor)]
+    L.idpd_precursor_count.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64)]
     L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
     L.idpd_set_chem.argtypes = [H, C.c_int32, C.POINTER(IdpdChemConfig)]
     L.idpd_chem_event.argtypes = [H, C.POINTER(C.c_int32)]
@@ -323,6 +325,19 @@ class Engine:
             skin = cur.skin
         self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach, skin=skin))),
                  "set_tuning")
+
+    def set_precursor(self, prop_from, prop_near, prop_to, threshold, seed, replica=0,
+                      enabled=True):
+        """Precursor conversion of the replica (idpd_set_precursor); threshold is
+        the u32 bound of the Saru draw (abi.precursor_threshold(p))."""
+        cfg = IdpdPrecursor(prop_from=prop_from, prop_near=prop_near, prop_to=prop_to,
+                            threshold=threshold, seed=seed, enabled=1 if enabled else 0)
+        self._ck(self.L.idpd_set_precursor(self.h, replica, C.byref(cfg)), "set_precursor")
+
+    def precursor_count(self, replica=0):
+        n = C.c_uint64()
+        self._ck(self.L.idpd_precursor_count(self.h, replica, C.byref(n)), "precursor_count")
+        return n.value
 
     def list_rebuilds(self):
         """Steps that rebuilt the cells and kept lists (0 with skin 0)."""

@@ -224,6 +224,30 @@ typedef struct idpd_chem_info {
 int idpd_chem_get_info(idpd_handle* h, int32_t replica, idpd_chem_info* info, uint32_t* targets,
                        int32_t cap);
 
+/* ---- precursor conversion (the reaction of the membrane-with-precursor
+ * workload; the reference's own reaction is ChemManager above) -------------
+ * Every step, after the force pass, each particle of property prop_from that
+ * has a particle of property prop_near within the cutoff (the step's pair
+ * set, r < 1) converts to prop_to when Saru(id, time, seed).u32() <
+ * threshold (threshold = p * 2^32 for a probability p per step; the Saru
+ * 3-seed constructor and u32() of saruprng.hpp:239-255, 322-333). Decisions
+ * read the properties of the start of the step, are integer and bit-exact,
+ * and take effect from the next step's pair passes. */
+typedef struct idpd_precursor {
+  uint32_t prop_from;   /* precursor property (IDPD_SOLVENT in that workload)  */
+  uint32_t prop_near;   /* property whose presence within the cutoff triggers
+                           the draw (IDPD_HYPHOB: a tail bead)                 */
+  uint32_t prop_to;     /* property after the conversion (IDPD_HYPHIL: a head)  */
+  uint32_t threshold;   /* converts when the draw is below it                   */
+  uint32_t seed;        /* third Saru seed                                       */
+  int32_t enabled;
+  int32_t reserved[2];
+} idpd_precursor;
+/* cfg NULL or enabled 0 switches the conversion off for that replica. */
+int idpd_set_precursor(idpd_handle* h, int32_t replica, const idpd_precursor* cfg);
+/* Conversions of the replica since its conversion was last set. */
+int idpd_precursor_count(idpd_handle* h, int32_t replica, uint64_t* conversions);
+
 /* ---- observables (Observer, observer.hpp:82-178) ---------------------------- */
 /* One macro observation of a replica, taken at the end of a step whose
  * Parameter::time is a multiple of the observation period (Parameter::step_mac,

@@ -322,6 +322,58 @@ int orc_density(const idpd_params* p, int32_t n, const double* pos, const uint32
   return 0;
 }
 
+/* ------------------------------------------------- precursor conversion */
+/* Saru 3-seed constructor and u32 (saruprng.hpp:239-255, 322-333) keyed on
+ * (id, time, seed); the pair test of pass 1 (nbdf_calculator.hpp:27-29). */
+int64_t orc_precursor(const idpd_params* p, int32_t n, const double* pos, const uint32_t* id,
+                      uint32_t* prop, uint32_t time, uint32_t from, uint32_t near, uint32_t to,
+                      uint32_t threshold, uint32_t seed, int32_t nthreads) {
+  orc_grid g;
+  if (grid_build(&g, n, pos, p->box) != 0) return -1;
+  uint8_t* conv = (uint8_t*)calloc(n > 0 ? n : 1, 1);
+  (void)nthreads;
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int32_t c = 0; c < g.ncell; c++) {
+    const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    for (int32_t m = g.start[c]; m < g.start[c + 1]; m++) {
+      const int32_t i = g.members[m];
+      if (prop[i] != from) continue;
+      const double rix = pos[3 * i], riy = pos[3 * i + 1], riz = pos[3 * i + 2];
+      int found = 0;
+      for (int dz = -1; dz <= 1 && !found; dz++)
+        for (int dy = -1; dy <= 1 && !found; dy++)
+          for (int dx = -1; dx <= 1 && !found; dx++) {
+            double sh[3];
+            const int32_t cj = nbr_cell(&g, p->box, cx, cy, cz, dx, dy, dz, sh);
+            for (int32_t mj = g.start[cj]; mj < g.start[cj + 1]; mj++) {
+              const int32_t j = g.members[mj];
+              if (j == i || prop[j] != near) continue;
+              const double ddx = rix - (pos[3 * j] + sh[0]), ddy = riy - (pos[3 * j + 1] + sh[1]),
+                           ddz = riz - (pos[3 * j + 2] + sh[2]);
+              if (ddx * ddx + ddy * ddy + ddz * ddz < 1.0) {
+                found = 1;
+                break;
+              }
+            }
+          }
+      if (found) {
+        orc_saru r;
+        saru_seed3(&r, id[i], time, seed);
+        conv[i] = saru_next(&r) < threshold;
+      }
+    }
+  }
+  int64_t count = 0;
+  for (int32_t i = 0; i < n; i++)
+    if (conv[i]) {
+      prop[i] = to;
+      count++;
+    }
+  free(conv);
+  grid_free(&g);
+  return count;
+}
+
 /* --------------------------------------------------------------- pass 2 */
 /* CalcForceEpEpDPD::operator() (nbdf_calculator.hpp:63-145) and
  * FPDPD::copyFromForce(RESULT::ForceDPD) (ptcl_class.hpp:48-51). */

@@ -94,6 +94,17 @@ int orc_chem_event(const idpd_params* p, const idpd_chem_params* cp, orc_mt* g, 
 
 /* All ordered pairs (i, j), i != j, within rc under the minimum image
  * (test/nearlist/near_list.cpp:69-92). Returns the count; writes at most cap. */
+/* The precursor conversion of the membrane-with-precursor workload (no
+ * reference function: the engine's idpd_precursor): every i with
+ * prop[i] == from and some j != i with prop[j] == near within r < 1 (the
+ * FP64 pair expression of pass 1) converts to `to` when the Saru(id_i, time,
+ * seed) u32 draw is below threshold. Decisions read the properties on entry;
+ * prop is updated in place. Returns the number of conversions, -1 when the
+ * box is too small for the cell grid. */
+int64_t orc_precursor(const idpd_params* p, int32_t n, const double* pos, const uint32_t* id,
+                      uint32_t* prop, uint32_t time, uint32_t from, uint32_t near, uint32_t to,
+                      uint32_t threshold, uint32_t seed, int32_t nthreads);
+
 int64_t orc_pairs_naive(int32_t n, const double* pos, const double* box, double rc,
                         uint32_t* pi, uint32_t* pj, int64_t cap);
 

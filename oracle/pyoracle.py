@@ -60,6 +60,10 @@ def lib():
                                      C.POINTER(OrcMT), C.POINTER(C.c_int32), C.c_int32, D, D, D, D,
                                      D, U, U, U, U, D, U, C.c_int32, U, C.POINTER(C.c_uint32),
                                      C.c_void_p, C.POINTER(C.c_int32)]
+        L.orc_precursor.restype = C.c_int64
+        L.orc_precursor.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, U, U, C.c_uint32,
+                                    C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                    C.c_int32]
         L.orc_pairs_naive.restype = C.c_int64
         L.orc_pairs_naive.argtypes = [C.c_int32, D, D, C.c_double, U, U, C.c_int64]
         _lib = L
@@ -226,6 +230,17 @@ def chem_event(p, cp, g, st, nei_cm, topol, core_ptcl_id, n_cap):
     out.update(pos=pos[:m], vel=vel[:m], acc=acc[:m], dsr=dsr[:m], id=pid[:m], prop=prop[:m],
                amp_id=amp_id[:m], unit=unit[:m])
     return rc, amp_out.value, targets[: 2 * nt.value].reshape(-1, 2), out
+
+
+def precursor(p, pos, pid, prop, time, from_, near, to, threshold, seed, nthreads=1):
+    """Precursor conversion (orc_precursor); returns (new prop, conversions)."""
+    out = np.ascontiguousarray(prop, np.uint32).copy()
+    cnt = lib().orc_precursor(C.byref(p), len(pos), np.ascontiguousarray(pos, np.float64),
+                              np.ascontiguousarray(pid, np.uint32), out, time, from_, near, to,
+                              threshold, seed, nthreads)
+    if cnt < 0:
+        raise ValueError("box too small for the cell grid")
+    return out, int(cnt)
 
 
 def pairs_naive(pos, box, rc=1.0):

@@ -14,7 +14,8 @@ import pyoracle as O
 from implicit_dpd_gb300 import build as B
 from implicit_dpd_gb300 import configs
 from implicit_dpd_gb300.abi import (IdpdChemConfig, IdpdChemInfo, IdpdChemParams, IdpdConfig,
-                                    IdpdObservation, IdpdParams, IdpdRunParam, params_to_dict)
+                                    IdpdObservation, IdpdParams, IdpdPrecursor, IdpdRunParam,
+                                    params_to_dict)
 from implicit_dpd_gb300.engine import EXPORTS, load
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -46,12 +47,13 @@ def test_struct_layouts_match_c():
 #include <stddef.h>
 #include "idpd_engine.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(idpd_params), sizeof(idpd_run_param),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(idpd_params), sizeof(idpd_run_param),
          sizeof(idpd_chem_params), sizeof(idpd_config), offsetof(idpd_params, seed),
          offsetof(idpd_params, cf_m), sizeof(idpd_chem_config),
          offsetof(idpd_chem_config, reserve_amp), sizeof(idpd_chem_info),
          offsetof(idpd_chem_info, core_raw), sizeof(idpd_observation),
-         offsetof(idpd_observation, bonded_virial));
+         offsetof(idpd_observation, bonded_virial), sizeof(idpd_precursor),
+         offsetof(idpd_precursor, enabled));
   return 0;
 }
 """
@@ -66,7 +68,8 @@ int main(void) {
             C.sizeof(IdpdConfig), IdpdParams.seed.offset, IdpdParams.cf_m.offset,
             C.sizeof(IdpdChemConfig), IdpdChemConfig.reserve_amp.offset, C.sizeof(IdpdChemInfo),
             IdpdChemInfo.core_raw.offset, C.sizeof(IdpdObservation),
-            IdpdObservation.bonded_virial.offset]
+            IdpdObservation.bonded_virial.offset, C.sizeof(IdpdPrecursor),
+            IdpdPrecursor.enabled.offset]
     assert got == want
 
 
