@@ -582,6 +582,31 @@ __device__ __forceinline__ float near_cut_w(float4 pi, float4 li, float4 pj, flo
   return w2 / (1.0f + dr);
 }
 
+// The pair vector of a close pair from the double-float cell-local
+// coordinates: the FP32 difference of the hi parts carries an absolute error
+// near 1e-7, which is a large part of a vector a few hundredths long.
+__device__ __forceinline__ void close_pair_vector(float4 pi, float4 li, float4 pj, float4 lj, int dx,
+                                                  int dy, int dz, const RepDev* R, float& ex,
+                                                  float& ey, float& ez) {
+  const float hi_i[3] = {pi.x, pi.y, pi.z}, lo_i[3] = {li.x, li.y, li.z};
+  const float hi_j[3] = {pj.x, pj.y, pj.z}, lo_j[3] = {lj.x, lj.y, lj.z};
+  const int dk[3] = {dx, dy, dz};
+  float e[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float e1, e2;
+    const float s = two_sum(hi_i[k], -hi_j[k], e1);
+    const float t = two_sum(s, -(float)dk[k] * R->cs_f[k], e2);
+    e[k] = t + (e1 + e2 + (lo_i[k] - lo_j[k]) - (float)dk[k] * R->cs_lo[k]);
+  }
+  ex = e[0];
+  ey = e[1];
+  ez = e[2];
+}
+
+// Pairs closer than 0.1 take their pair vector from close_pair_vector.
+constexpr float kCloseCut2 = 0.01f;
+
 // The particle of one warp in pass 2 and its fixed-point sums.
 struct PairI {
   float4 pi, vi, di;
@@ -621,10 +646,15 @@ __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, c
   if (idj == I.idi) return false;  // nbdf_calculator.hpp:84
   const float4 pj = __ldg(d.posf + t);
   const float4 dj = __ldg(d.densf + t);
-  const float ex = (I.pi.x - (float)dx * I.csx) - pj.x;
-  const float ey = (I.pi.y - (float)dy * I.csy) - pj.y;
-  const float ez = (I.pi.z - (float)dz * I.csz) - pj.z;
-  const float dr2 = ex * ex + ey * ey + ez * ez;
+  float ex = (I.pi.x - (float)dx * I.csx) - pj.x;
+  float ey = (I.pi.y - (float)dy * I.csy) - pj.y;
+  float ez = (I.pi.z - (float)dz * I.csz) - pj.z;
+  float dr2 = ex * ex + ey * ey + ez * ez;
+  if (dr2 < kCloseCut2) {
+    close_pair_vector(I.pi, __ldg(d.poslo + I.row), pj, __ldg(d.poslo + t), dx, dy, dz, R, ex, ey,
+                      ez);
+    dr2 = ex * ex + ey * ey + ez * ez;
+  }
   const float inv_dr = rsqrtf(dr2);
   const float dr = dr2 * inv_dr;
   float w = 1.0f - dr;
