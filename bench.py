@@ -513,13 +513,29 @@ def run_engine(args, rank, world, local_rank):
         eq = e.download()
         st64 = dict(st, pos=eq["pos"], vel=eq["vel"], acc=eq["acc"])
         e64 = make_engine(st64, n_amp, rp, flags=CFG_FP64_PAIRS, device=local_rank)
+        # the stated force error: both pair passes on the timed state, FP32
+        # engine against the plain FP64 kernels
+        e32 = make_engine(st64, n_amp, rp, device=local_rank)
+        for x in (e32, e64):
+            x.density()
+            x.force()
+        f32, f64 = e32.download()["acc"], e64.download()["acc"]
+        e32.close()
+        mag = np.linalg.norm(f64, axis=1)
+        floor = np.sqrt(np.mean(mag ** 2))
+        err = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, floor)
+        force_err = {"max_rel": float(err.max()),
+                     "aggregate": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+                     "bar": 1e-5,
+                     "definition": "per particle |F32 - F64| / max(|F64|, rms |F64|), pair "
+                                   "forces of the timed state, plain FP64 kernels as reference"}
         e64.step(1)
         k64 = max(2, min(args.steps, 10))
         e64.step(k64)
         ms64 = e64.last_step_ms()
         v64 = n * k64 / (ms64 * 1e-3)
         fp64 = {"value": v64, "unit": "particle-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
-                "speedup_fp32_over_fp64": value / world / v64}
+                "speedup_fp32_over_fp64": value / world / v64, "force_error": force_err}
         e64.close()
 
     # end to end through the C ABI: host pinned pos/vel/acc in, one step, out

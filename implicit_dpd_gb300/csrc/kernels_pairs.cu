@@ -619,7 +619,7 @@ struct PairI {
 
 // A lane's share of one fixed-point sum of pass 2 as the sums of the
 // fix_force_parts of its terms. A list gives a lane at most kNbrCap / 32
-// terms, so the parts' warp totals stay below 2^29 and reduce in 32 bits.
+// terms, so the parts' warp totals stay below 2^30 and reduce in 32 bits.
 struct FixSum {
   int hi, lo;
   __device__ __forceinline__ void add(float v, bool& range) {
