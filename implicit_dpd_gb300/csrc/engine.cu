@@ -221,6 +221,13 @@ void fill_repdev(RepDev& R, const idpd_params& p, int reach, float skin) {
   R.dens_unscale_f = (float)R.dens_unscale;
 }
 
+// Bit f set when some replica uses pair-force form f.
+int form_mask(const idpd_handle* h) {
+  int m = 0;
+  for (int r = 0; r < h->R; r++) m |= 1 << h->params[r].form;
+  return m;
+}
+
 // fill_repdev plus the replica's precursor conversion.
 void fill_rep(const idpd_handle* h, int r, RepDev& R) {
   fill_repdev(R, h->params[r], h->tune.reach, h->tune.skin);
@@ -653,7 +660,7 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
-  launch_force(d, h->nblk, fp64, observe, h->tune, h->st);
+  launch_force(d, h->nblk, fp64, observe, h->tune, form_mask(h), h->st);
   if (h->prec_any) {
     d.prec_count = h->prec_dev;
     launch_precursor(d, h->nblk, !fp64, h->st);
@@ -1142,7 +1149,7 @@ int idpd_force(idpd_handle* h) {
   if (!h->density_valid) return fail(h, IDPD_ERR_STATE, "idpd_force needs idpd_density on the same positions");
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
-  launch_force(h->d, h->nblk, fp64, true, h->tune, h->st);
+  launch_force(h->d, h->nblk, fp64, true, h->tune, form_mask(h), h->st);
   launch_fq_to_acc(h->d, h->nblk, h->press64, h->st);
   return check_device_error(h);
 }
@@ -1341,7 +1348,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[4], h->st));
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_force(d, h->nblk, fp64, false, h->tune, h->st);
+  launch_force(d, h->nblk, fp64, false, h->tune, form_mask(h), h->st);
   CK(cudaEventRecord(ev[6], h->st));
   launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[7], h->st));

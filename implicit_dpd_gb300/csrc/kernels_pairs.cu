@@ -612,7 +612,6 @@ struct PairI {
   float4 pi, vi, di;
   uint32_t idi, pri, seed;
   int row;  // the particle's row (its low position parts are read near the cutoff)
-  int form;
   float csx, csy, csz;
   long long fx, fy, fz, px, py, pz;
 };
@@ -637,7 +636,7 @@ struct FixSum {
 static_assert((kNbrCap / 32) * (1 << 21) < (1 << 26), "32-bit warp totals of the fixed-point parts");
 
 // The force and virial terms of one pair (the pair arithmetic of pass 2).
-template <bool PRESS>
+template <bool PRESS, bool CHECK, int FORM>
 __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, const PairTables& T,
                                            const PairI& I, int t, int dx, int dy, int dz,
                                            float g[6]) {
@@ -661,9 +660,11 @@ __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, c
   if (dr2 > kNearCut2)  // admitted pairs have 1 - r >= 0 up to ~1e-13
     w = fmaxf(near_cut_w(I.pi, __ldg(d.poslo + I.row), pj, __ldg(d.poslo + t), dx, dy, dz, R, dr),
               0.0f);
-  const float a = pair_all_cf(T, R, I.form, I.pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, I.vi, vj,
-                              I.di, dj, I.idi, idj, I.seed);
-  if (!isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
+  const float a = pair_cf<FORM>(T, R, I.pri, fbits(pj.w), dr, inv_dr, w, ex, ey, ez, I.vi, vj,
+                                I.di, dj, I.idi, idj, I.seed);
+  // a non-finite term fails the range test of the 32-bit parts, and the 64-bit
+  // pass (CHECK) reports it
+  if (CHECK && !isfinite(a)) atomicCAS(d.err, 0, kErrNonFinite);
   g[0] = a * ex;
   g[1] = a * ey;
   g[2] = a * ez;
@@ -676,22 +677,22 @@ __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, c
 }
 
 // One pair term added to the particle's sums in 32-bit parts.
-template <bool PRESS>
+template <bool PRESS, int FORM>
 __device__ __forceinline__ void eval_pair_parts(const DevState& d, const RepDev* R,
                                                 const PairTables& T, const PairI& I, int t, int dx,
                                                 int dy, int dz, FixSum f[6], bool& range) {
   float g[6];
-  if (!pair_terms<PRESS>(d, R, T, I, t, dx, dy, dz, g)) return;
+  if (!pair_terms<PRESS, false, FORM>(d, R, T, I, t, dx, dy, dz, g)) return;
 #pragma unroll
   for (int c = 0; c < (PRESS ? 6 : 3); c++) f[c].add(g[c], range);
 }
 
 // One pair term added to the particle's sums (the lane's share).
-template <bool PRESS>
+template <bool PRESS, int FORM>
 __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, const PairTables& T,
                                           PairI& I, int t, int dx, int dy, int dz) {
   float g[6];
-  if (!pair_terms<PRESS>(d, R, T, I, t, dx, dy, dz, g)) return;
+  if (!pair_terms<PRESS, true, FORM>(d, R, T, I, t, dx, dy, dz, g)) return;
   I.fx += fix_force(g[0]);
   I.fy += fix_force(g[1]);
   I.fz += fix_force(g[2]);
@@ -704,22 +705,17 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
 
 // One warp per particle. The list of pass 1 gives the pairs, 32 per round
 // with every lane busy; a particle whose list overflowed walks its cells
-// again and queues the in-range pairs in shared memory.
-template <int REACH, bool PRESS>
+// again and queues the in-range pairs in shared memory. One launch per pair
+// form present: a block whose replica has another form returns at once.
+template <int REACH, bool PRESS, int FORM>
 __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t qt[kWarps][64], qc[kWarps][64];
   __shared__ PairTables T;
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
-  for (int k = threadIdx.x; k < 54; k += blockDim.x) {
-    float v;
-    if (k < 9) v = R->cf_c[k];
-    else if (k < 18) v = R->cf_g[k - 9];
-    else if (k < 27) v = R->cf_r[k - 18];
-    else v = R->cf_m[k - 27];
-    (&T.cf_c[0])[k] = v;
-  }
+  if (R->form != FORM) return;
+  if (threadIdx.x < 9) fill_pair_table(T, *R, threadIdx.x);
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
@@ -729,7 +725,6 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   const int s_end = min(s0 + 32, R->row_off + R->n);
   PairI I;
   I.seed = R->seed + d.rep_time[r];
-  I.form = R->form;
   I.csx = R->cs_f[0];
   I.csy = R->cs_f[1];
   I.csz = R->cs_f[2];
@@ -756,7 +751,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
         if (k + 32 < (int)cnt) e_next = list[k + 32];
         int t, dx, dy, dz;
         read_entry(e, t, dx, dy, dz);
-        eval_pair_parts<PRESS>(d, R, T, I, t, dx, dy, dz, f, range);
+        eval_pair_parts<PRESS, FORM>(d, R, T, I, t, dx, dy, dz, f, range);
       }
       if (__all_sync(0xffffffffu, range)) {
         const long long fx = f[0].total(), fy = f[1].total(), fz = f[2].total();
@@ -786,7 +781,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
       for (int k = lane; k < (int)cnt; k += 32) {
         int t, dx, dy, dz;
         read_entry(list[k], t, dx, dy, dz);
-        eval_pair<PRESS>(d, R, T, I, t, dx, dy, dz);
+        eval_pair<PRESS, FORM>(d, R, T, I, t, dx, dy, dz);
       }
     } else {
       const int cell = (int)d.scell[s];
@@ -835,7 +830,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
           if (qn >= 32) {
             __syncwarp();
             const PairCode pc = unpack_code(QC[lane]);
-            eval_pair<PRESS>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+            eval_pair<PRESS, FORM>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
             __syncwarp();
             if (lane < qn - 32) {
               QT[lane] = QT[32 + lane];
@@ -849,7 +844,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
       __syncwarp();
       if (lane < qn) {
         const PairCode pc = unpack_code(QC[lane]);
-        eval_pair<PRESS>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+        eval_pair<PRESS, FORM>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
       }
       __syncwarp();
     }
@@ -951,8 +946,23 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
   }
 }
 
+template <int FORM>
+void launch_force_form(const DevState& d, int nblk, bool with_press, int reach, cudaStream_t st) {
+  if (reach == 2) {
+    if (with_press)
+      k_force_f32<2, true, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+    else
+      k_force_f32<2, false, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+  } else {
+    if (with_press)
+      k_force_f32<1, true, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+    else
+      k_force_f32<1, false, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+  }
+}
+
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  cudaStream_t st) {
+                  int form_mask, cudaStream_t st) {
   if (nblk == 0) return;
   if (fp64) {
     if (with_press)
@@ -961,17 +971,12 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
       k_force_f64<false><<<nblk, kRowBlock, 0, st>>>(d);
     return;
   }
-  if (tu.reach == 2) {
-    if (with_press)
-      k_force_f32<2, true><<<nblk, kRowBlock, 0, st>>>(d);
-    else
-      k_force_f32<2, false><<<nblk, kRowBlock, 0, st>>>(d);
-  } else {
-    if (with_press)
-      k_force_f32<1, true><<<nblk, kRowBlock, 0, st>>>(d);
-    else
-      k_force_f32<1, false><<<nblk, kRowBlock, 0, st>>>(d);
-  }
+  if (form_mask & (1 << IDPD_FORM_MDPD_K))
+    launch_force_form<IDPD_FORM_MDPD_K>(d, nblk, with_press, tu.reach, st);
+  if (form_mask & (1 << IDPD_FORM_PAIRWISE_K))
+    launch_force_form<IDPD_FORM_PAIRWISE_K>(d, nblk, with_press, tu.reach, st);
+  if (form_mask & (1 << IDPD_FORM_WARREN_K))
+    launch_force_form<IDPD_FORM_WARREN_K>(d, nblk, with_press, tu.reach, st);
 }
 
 // ------------------------------------------- precursor conversion

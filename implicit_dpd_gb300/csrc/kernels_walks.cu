@@ -409,12 +409,7 @@ int walk_dispatch(WalkState* s, cudaStream_t st, const RepDev& R, const idpd_par
     const unsigned nb = (unsigned)((ni + kWalkWarps - 1) / kWalkWarps);
     if (dpd) {
       PairTables T;
-      for (int k = 0; k < 9; k++) {
-        T.cf_c[k] = R.cf_c[k];
-        T.cf_g[k] = R.cf_g[k];
-        T.cf_r[k] = R.cf_r[k];
-      }
-      for (int k = 0; k < 27; k++) T.cf_m[k] = R.cf_m[k];
+      for (int k = 0; k < 9; k++) fill_pair_table(T, R, k);
       k_walk_force<<<nb, 32 * kWalkWarps, 0, st>>>(W, R, T, p.seed + p.time);
     } else {
       k_walk_density<<<nb, 32 * kWalkWarps, 0, st>>>(W, R);

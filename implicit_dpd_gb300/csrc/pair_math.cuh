@@ -16,36 +16,63 @@ __device__ __forceinline__ uint32_t dens_weight(float dr2, bool warren, float in
   return (uint32_t)(__float_as_int(fmaf(w, pre, 1.0f)) - 0x3f800000);
 }
 
+// The replica's FP32 coefficients per property pair k = 3 prop_i + prop_j,
+// packed so that one pair reads two shared-memory words: a = (cf_c, cf_r,
+// cf_g, cf_m[k][0]), b = (cf_m[k][1], cf_m[k][2]).
 struct PairTables {
-  float cf_c[9], cf_g[9], cf_r[9], cf_m[27];
+  float4 a[9];
+  float2 b[9];
 };
 
+__host__ __device__ __forceinline__ void fill_pair_table(PairTables& T, const RepDev& R, int k) {
+  T.a[k] = make_float4(R.cf_c[k], R.cf_r[k], R.cf_g[k], R.cf_m[3 * k]);
+  T.b[k] = make_float2(R.cf_m[3 * k + 1], R.cf_m[3 * k + 2]);
+}
+
 // Conservative + random + dissipative magnitude over dr for one pair
-// (nbdf_calculator.hpp:108-132), FP32. dr, 1/dr and w = 1 - dr are passed in.
-__device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* R, int form,
-                                             uint32_t pri, uint32_t prj, float dr, float inv_dr,
-                                             float w, float ex, float ey, float ez, float4 vi,
-                                             float4 vj, float4 di, float4 dj, uint32_t idi,
-                                             uint32_t idj, uint32_t seed) {
+// (nbdf_calculator.hpp:108-132), FP32, for the pair-force form FORM. dr, 1/dr
+// and w = 1 - dr are passed in.
+template <int FORM>
+__device__ __forceinline__ float pair_cf(const PairTables& T, const RepDev* R, uint32_t pri,
+                                         uint32_t prj, float dr, float inv_dr, float w, float ex,
+                                         float ey, float ez, float4 vi, float4 vj, float4 di,
+                                         float4 dj, uint32_t idi, uint32_t idj, uint32_t seed) {
   const float sqw = w > 0.0f ? w * rsqrtf(w) : 0.0f;  // sqrt(1 - r), 2 ulp
   const int k = pri * 3 + prj;
+  const float4 ta = T.a[k];
   float cons;
-  if (form == IDPD_FORM_PAIRWISE_K) {
+  if constexpr (FORM == IDPD_FORM_PAIRWISE_K) {
     cons = 25.0f * w;
-  } else if (form == IDPD_FORM_WARREN_K) {
+  } else if constexpr (FORM == IDPD_FORM_WARREN_K) {
     const float rho = (di.x + dj.x) + (di.y + dj.y) + (di.z + dj.z);
     const float wb = dr < R->wrd ? 1.0f - dr * R->winv_rd : 0.0f;
     cons = R->wa * w + R->wb * rho * wb;
   } else {
-    const float cf_pair = dr >= kArc ? T.cf_c[k] * (dr - kArc) : 0.0f;
-    const float cf_mbd = T.cf_m[3 * k] * (di.x + dj.x) + T.cf_m[3 * k + 1] * (di.y + dj.y) +
-                         T.cf_m[3 * k + 2] * (di.z + dj.z);
+    const float2 tb = T.b[k];
+    const float cf_pair = dr >= kArc ? ta.x * (dr - kArc) : 0.0f;
+    const float cf_mbd = ta.w * (di.x + dj.x) + tb.x * (di.y + dj.y) + tb.y * (di.z + dj.z);
     cons = (cf_pair + cf_mbd) * w;
   }
   Saru sr(idi < idj ? idi : idj, idi < idj ? idj : idi, seed);
   const float rnd = saru_nrml_f32(sr);
   const float ddv = ex * (vi.x - vj.x) + ey * (vi.y - vj.y) + ez * (vi.z - vj.z);
-  return (cons + T.cf_r[k] * sqw * rnd - T.cf_g[k] * w * ddv * inv_dr) * inv_dr;
+  return (cons + ta.y * sqw * rnd - ta.z * w * ddv * inv_dr) * inv_dr;
+}
+
+// pair_cf with the form chosen at run time.
+__device__ __forceinline__ float pair_all_cf(const PairTables& T, const RepDev* R, int form,
+                                             uint32_t pri, uint32_t prj, float dr, float inv_dr,
+                                             float w, float ex, float ey, float ez, float4 vi,
+                                             float4 vj, float4 di, float4 dj, uint32_t idi,
+                                             uint32_t idj, uint32_t seed) {
+  if (form == IDPD_FORM_PAIRWISE_K)
+    return pair_cf<IDPD_FORM_PAIRWISE_K>(T, R, pri, prj, dr, inv_dr, w, ex, ey, ez, vi, vj, di,
+                                         dj, idi, idj, seed);
+  if (form == IDPD_FORM_WARREN_K)
+    return pair_cf<IDPD_FORM_WARREN_K>(T, R, pri, prj, dr, inv_dr, w, ex, ey, ez, vi, vj, di, dj,
+                                       idi, idj, seed);
+  return pair_cf<IDPD_FORM_MDPD_K>(T, R, pri, prj, dr, inv_dr, w, ex, ey, ez, vi, vj, di, dj, idi,
+                                   idj, seed);
 }
 
 // Pairs with dr^2 above this take w = 1 - dr from the compensated path.

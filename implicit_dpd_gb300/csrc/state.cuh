@@ -161,7 +161,7 @@ void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verl
 void launch_precursor(const DevState& d, int nblk, bool lists, cudaStream_t st);
 void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  cudaStream_t st);
+                  int form_mask, cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
 
 // kernels_chem.cu: one RandomChemEvent (LOCAL_CHEM_EVENT form) on replica 0.
