@@ -948,14 +948,16 @@ int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double
   const RepDev& R = h->reps_h[r];
   const size_t n = (size_t)R.n;
   if (n == 0) return IDPD_OK;
-  // three strided copies interleave pos/vel/acc into 9 doubles per row
-  const size_t row = 9 * sizeof(double), w = 3 * sizeof(double);
-  CK(cudaMemcpy2DAsync(h->xfer, row, pos, w, w, n, cudaMemcpyHostToDevice, h->st));
-  CK(cudaMemcpy2DAsync(h->xfer + 3, row, vel, w, w, n, cudaMemcpyHostToDevice, h->st));
-  CK(cudaMemcpy2DAsync(h->xfer + 6, row, acc, w, w, n, cudaMemcpyHostToDevice, h->st));
-  launch_set_dynamics(h->d, h->xfer, R.row_off, R.n, R.box[0], R.box[1], R.box[2], h->st);
+  // three contiguous copies: pos, vel, acc one after the other
+  const size_t bytes = 3 * n * sizeof(double);
+  CK(cudaMemcpyAsync(h->xfer, pos, bytes, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->xfer + 3 * n, vel, bytes, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->xfer + 6 * n, acc, bytes, cudaMemcpyHostToDevice, h->st));
+  // with built kept lists the position change counts as displacement (the
+  // next step rebuilds when it is too large); else the lists are rebuilt
+  const bool kept = h->d.vdev && !h->vl_dirty && h->tune.skin > 0.0f;
+  launch_set_dynamics(h->d, h->xfer, R.row_off, R.n, R.box[0], R.box[1], R.box[2], kept, h->st);
   h->density_valid = false;
-  h->vl_dirty = true;  // new positions: the kept lists are rebuilt
   return IDPD_OK;
 }
 
@@ -1021,16 +1023,15 @@ int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, dou
   const RepDev& R = h->reps_h[r];
   const int n = R.n;
   if (n == 0) return IDPD_OK;
-  double* tmp = nullptr;
-  CK(cudaMallocAsync((void**)&tmp, sizeof(double) * 3 * (size_t)n, h->st));
   const DevState& d = h->d;
   struct F { const double *x, *y, *z; double* out; } f3[3] = {
       {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
   int rc = IDPD_OK;
-  for (auto& f : f3) {
-    if (!f.out) continue;
-    launch_soa_to_aos(f.x, f.y, f.z, d.orig, R.row_off, tmp, n, h->st);
-    cudaError_t e = cudaMemcpyAsync(f.out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
+  for (int k = 0; k < 3; k++) {  // into the staging buffer, then one copy each
+    if (!f3[k].out) continue;
+    double* tmp = h->xfer + 3 * (size_t)n * k;
+    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.orig, R.row_off, tmp, n, h->st);
+    cudaError_t e = cudaMemcpyAsync(f3[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
     if (e != cudaSuccess) rc = fail(h, IDPD_ERR_CUDA, "download: %s", cudaGetErrorString(e));
   }
   const uint32_t* uf[4] = {d.id, d.prop, d.amp_id, d.unit};
@@ -1047,7 +1048,6 @@ int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, dou
     CK(cudaStreamSynchronize(h->st));
     for (int q = 0; q < n; q++) uo[k][orig[q] - (uint32_t)R.row_off] = tmpu[q];
   }
-  CK(cudaFreeAsync(tmp, h->st));
   CK(cudaStreamSynchronize(h->st));
   return rc;
 }

@@ -324,30 +324,46 @@ void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n
   k_aos_to_soa<<<(n + 255) / 256, 256, 0, st>>>(aos, x, y, z, n);
 }
 
-// Per-step host exchange: rows of one replica in upload order, 9 doubles
-// each (pos, vel, acc), into the storage rows; invalid rows raise an error.
-__global__ void k_set_dynamics(DevState d, const double* aos, int row0, int n, double b0, double b1,
-                               double b2) {
+// Per-step host exchange: rows of one replica in upload order (pos, vel and
+// acc as three arrays of 3 doubles per row) into the storage rows; invalid
+// rows raise an error. The position change of a row counts, at its nearest
+// image, as displacement for the kept lists (the delta_sumr of their last
+// rebuild moves back by it), so a host that hands back the positions it read
+// keeps the lists, and one that moves particles far enough triggers a rebuild.
+__global__ void k_set_dynamics(DevState d, const double* xfer, int row0, int n, double b0,
+                               double b1, double b2, int kept) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t i = d.loc[row0 + k];
-  const double* a = aos + 9 * (size_t)k;
+  const double* p = xfer + 3 * (size_t)k;
+  const double* v = xfer + 3 * ((size_t)n + k);
+  const double* a = xfer + 3 * (2 * (size_t)n + k);
   const double box[3] = {b0, b1, b2};
   bool ok = true;
 #pragma unroll
-  for (int c = 0; c < 3; c++) ok = ok && a[c] >= 0.0 && a[c] <= box[c];
-#pragma unroll
-  for (int c = 3; c < 9; c++) ok = ok && isfinite(a[c]);
+  for (int c = 0; c < 3; c++) ok = ok && p[c] >= 0.0 && p[c] <= box[c] && isfinite(v[c]) && isfinite(a[c]);
   if (!ok) atomicCAS(d.err, 0, kErrBadCell);
-  d.px[i] = a[0]; d.py[i] = a[1]; d.pz[i] = a[2];
-  d.vx[i] = a[3]; d.vy[i] = a[4]; d.vz[i] = a[5];
-  d.ax[i] = a[6]; d.ay[i] = a[7]; d.az[i] = a[8];
+  if (kept) {
+    const uint32_t s = d.rank[i];
+    const double old[3] = {d.px[i], d.py[i], d.pz[i]};
+    double* dr[3] = {d.drx, d.dry, d.drz};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double e = p[c] - old[c];
+      e = e > 0.5 * box[c] ? e - box[c] : (e < -0.5 * box[c] ? e + box[c] : e);
+      dr[c][s] -= e;
+    }
+  }
+  d.px[i] = p[0]; d.py[i] = p[1]; d.pz[i] = p[2];
+  d.vx[i] = v[0]; d.vy[i] = v[1]; d.vz[i] = v[2];
+  d.ax[i] = a[0]; d.ay[i] = a[1]; d.az[i] = a[2];
 }
 
-void launch_set_dynamics(const DevState& d, const double* aos, int row0, int n, double box0,
-                         double box1, double box2, cudaStream_t st) {
+void launch_set_dynamics(const DevState& d, const double* xfer, int row0, int n, double box0,
+                         double box1, double box2, bool kept, cudaStream_t st) {
   if (n == 0) return;
-  k_set_dynamics<<<(n + 255) / 256, 256, 0, st>>>(d, aos, row0, n, box0, box1, box2);
+  k_set_dynamics<<<(n + 255) / 256, 256, 0, st>>>(d, xfer, row0, n, box0, box1, box2,
+                                                  kept ? 1 : 0);
 }
 
 // Storage rows [row0, row0 + n) back to upload order: aos[orig - row0] = row.

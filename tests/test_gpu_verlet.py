@@ -78,3 +78,50 @@ def test_skin_needs_room_in_the_box():
     e.set_params(mdpd_params(box))
     with pytest.raises(EngineError, match="skin"):
         e.set_tuning(1, 2.5)
+
+
+@pytest.mark.parametrize("skin", [0.0, 0.3])
+def test_host_roundtrip_keeps_the_trajectory(skin):
+    """Positions, velocities and accelerations read back and handed in again
+    every step (the per-step host exchange) change nothing: the kept lists
+    stay (the position change is zero) and the states agree bit for bit."""
+    box, st, n_amp = mixed_system(seed=21)
+    p = mdpd_params(box, time=40)
+    a = _engine(p, st, n_amp, skin)
+    a.step(12)
+    b = _engine(p, st, n_amp, skin)
+    n = len(st["pos"])
+    pos, vel, acc = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+    for _ in range(12):
+        b.download_dynamics(pos, vel, acc)
+        b.set_dynamics(pos, vel, acc)
+        b.step(1)
+    sa, sb = a.download(), b.download()
+    for k in ("pos", "vel", "acc"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert a.list_rebuilds() == b.list_rebuilds()
+
+
+def test_host_move_past_half_the_skin_rebuilds():
+    """A particle moved by the host by more than half the skin (across the
+    periodic boundary) makes the next step rebuild, and that step matches the
+    oracle step from the state handed in."""
+    box, st, n_amp = mixed_system(seed=22)
+    p = mdpd_params(box, time=70)
+    e = _engine(p, st, n_amp, 0.2)
+    e.step(5)
+    s = e.download()
+    k = int(np.argmin(s["pos"][:, 0]))
+    pos = s["pos"].copy()
+    pos[k, 0] = np.mod(pos[k, 0] - 0.35, box[0])  # wraps to the far side
+    e.set_dynamics(pos, s["vel"], s["acc"])
+    r0 = e.list_rebuilds()
+    s0 = e.download()
+    assert np.array_equal(s0["pos"], pos)
+    t0 = e.get_params().time
+    e.step(1)
+    assert e.list_rebuilds() == r0 + 1
+    s1 = e.download()
+    ref = _oracle_step(p, s0, n_amp, t0)
+    assert np.array_equal(s1["pos"], ref["pos"])
+    assert rel_force_err(s1["acc"], ref["acc"])[0] < FORCE_TOL
