@@ -174,7 +174,7 @@ __device__ __forceinline__ void add_weight(uint32_t& q0, uint32_t& q1, uint32_t&
 // lists (VERLET): one pass over the particle's kept list tests each
 // candidate, adds its weight and appends it to the list of pass 2.
 template <int REACH, bool VERLET>
-__global__ void __launch_bounds__(kRowBlock) k_density_f32(DevState d) {
+__global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t lst[kWarps][kNbrCap];
   const int r = d.blk_rep[blockIdx.x];
