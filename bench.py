@@ -195,6 +195,21 @@ def profiled_traffic(name):
     return None
 
 
+def profiled_inst_per_bead(name):
+    """Warp instructions per bead of a kernel from its committed ncu summary
+    (smsp__inst_executed.sum of the captured launch over its beads)."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    inst, beads = None, None
+    for line in open(path):
+        if "`smsp__inst_executed.sum`" in line:
+            inst = float(line.split("|")[2].split()[0])
+        if line.startswith("DRAM traffic of the captured launch:"):
+            beads = float(line.split(" for ")[1].split()[0])
+    return inst / beads if inst and beads else None
+
+
 def equilibrated_patch(threads, equil=2000):
     """One bilayer of an 8 x 8 x 4.8 periodic patch of membrane_1m taken
     through `equil` oracle steps (the compaction the timed GPU state went
@@ -505,6 +520,22 @@ def run_engine(args, rank, world, local_rank):
                 "note": "the pair passes are bound by CUDA-core instruction issue (distance "
                         "tests, Saru hash, transcendentals per pair), not by HBM; the HBM "
                         "fraction is small by construction"}
+    # the bound the pair passes do meet: warp-instruction issue (4 per SM and
+    # clock), with the kernel's instructions per bead from its ncu capture
+    ipb = profiled_inst_per_bead(kinfo["profile"])
+    if ipb is not None:
+        import torch
+
+        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            ach = ipb * n / (top_ms * 1e-3)
+            peak_i = 4.0 * sms * mhz * 1e6
+            roofline["issue"] = {
+                "achieved": ach, "peak": peak_i, "unit": "warp instructions/s", "frac": ach / peak_i,
+                "inst_per_particle": ipb,
+                "source": "smsp__inst_executed.sum per bead of the committed ncu capture x N / the "
+                          "kernel's CUDA-event time; peak = 4 issue slots x SMs x median SM clock"}
     step_gbs = STEP_BYTES_PER_PARTICLE * n / (ms_max / args.steps * 1e-3) / 1e9
 
     # plain FP64 pair kernels on the same workload (the baseline of the metric)

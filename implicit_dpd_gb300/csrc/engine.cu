@@ -366,14 +366,6 @@ int ensure_verlet_ready(idpd_handle* h) {
   return IDPD_OK;
 }
 
-// The next step rebuilds the kept lists (their cells or rows changed).
-int force_list_rebuild(idpd_handle* h) {
-  static const int kOne = 1;
-  if (h->d.vdev) CK(cudaMemcpyAsync(&h->d.vdev->force, &kOne, sizeof(int), cudaMemcpyHostToDevice, h->st));
-  h->vl_dirty = false;
-  return IDPD_OK;
-}
-
 int ensure_aux(idpd_handle* h) {
   if (h->press64) return IDPD_OK;
   int rc = ensure_press(h);

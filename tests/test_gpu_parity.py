@@ -305,3 +305,27 @@ def test_dense_membrane_density_force_match_oracle(rho):
         e.force()
         worst, agg = rel_force_err(e.download()["acc"], acc)
         assert worst < FORCE_TOL, (reach, worst, agg)
+
+
+def test_replicas_of_different_pair_forms_batched_equal_single():
+    """Replicas with the MDPD, pairwise and Warren forms in one handle: pass 2
+    runs one launch per form present, each replica only in its own, and the
+    batch equals the single-replica handles bit for bit."""
+    box, st, n_amp = mixed_system(seed=31, box=(8.0, 8.0, 8.0), n_amp=200)
+    liq = configs.liquid(np.array([7.0, 7.0, 7.0]), 5.0, seed=32)
+    runs = [(mdpd_params(box, seed=11, time=3), st, n_amp),
+            (pairwise_params(np.array([7.0, 7.0, 7.0]), seed=12, time=4), liq, 0),
+            (warren_params(np.array([7.0, 7.0, 7.0]), seed=13, time=5), liq, 0)]
+    eb = Engine(n_replicas=3)
+    for k, (p, s, na) in enumerate(runs):
+        eb.set_params(p, k)
+        eb.upload(s, k)
+        if na:
+            eb.build_topology(na, [0], k)
+    eb.step(4)
+    for k, (p, s, na) in enumerate(runs):
+        es = engine_for(p, s, na, [0] if na else ())
+        es.step(4)
+        a, b = eb.download(k), es.download()
+        for key in ("pos", "vel", "acc"):
+            assert np.array_equal(a[key], b[key]), (k, key)
