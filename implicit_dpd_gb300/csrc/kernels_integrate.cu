@@ -250,16 +250,32 @@ __global__ void __launch_bounds__(kRowBlock) k_cm_partial(DevState d, int force_
   }
 }
 
-__global__ void k_cm_finalize(DevState d, int R_n, int force_now) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= R_n) return;
+// One block per replica sums its blocks' partial momenta (integers: any
+// order gives the same total).
+constexpr int kCmThreads = 256;
+__global__ void __launch_bounds__(kCmThreads) k_cm_finalize(DevState d, int force_now) {
+  __shared__ long long sh[3][kCmThreads / 32];
+  const int r = blockIdx.x;
   if (!cm_due(d, r, force_now)) return;
   const RepDev* R = d.reps + r;
   const long long* part = reinterpret_cast<const long long*>(d.blk_part);
   long long s[3] = {0, 0, 0};
-  for (int b = R->blk_off; b < R->blk_off + R->nblk; b++)
+  for (int b = R->blk_off + threadIdx.x; b < R->blk_off + R->nblk; b += kCmThreads)
     for (int k = 0; k < 3; k++) s[k] += part[3 * b + k];
-  for (int k = 0; k < 3; k++) d.rep_mean[3 * r + k] = ((double)s[k] / kVelScale) / (double)R->n;
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int k = 0; k < 3; k++) sh[k][w] = s[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 3; k++) {
+      long long t = 0;
+      for (int q = 0; q < kCmThreads / 32; q++) t += sh[k][q];
+      d.rep_mean[3 * r + k] = ((double)t / kVelScale) / (double)R->n;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kRowBlock) k_cm_apply(DevState d, int force_now) {
@@ -276,7 +292,7 @@ __global__ void __launch_bounds__(kRowBlock) k_cm_apply(DevState d, int force_no
 void launch_cmdrift(const DevState& d, int nblk, int R, bool force_now, cudaStream_t st) {
   if (nblk == 0) return;
   k_cm_partial<<<nblk, kRowBlock, 0, st>>>(d, force_now ? 1 : 0);
-  k_cm_finalize<<<(R + 127) / 128, 128, 0, st>>>(d, R, force_now ? 1 : 0);
+  k_cm_finalize<<<R, kCmThreads, 0, st>>>(d, force_now ? 1 : 0);
   k_cm_apply<<<nblk, kRowBlock, 0, st>>>(d, force_now ? 1 : 0);
 }
 
