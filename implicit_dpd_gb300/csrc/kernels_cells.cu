@@ -2,6 +2,8 @@
 // copies that the pair passes read. Replaces the FDPS tree build and the j
 // gather of TreeForForceShort::Gather (src/main.cpp:124-132, 173-174) and
 // performs drift_and_predict (driftkick.hpp:6-27) in the same pass.
+#include <algorithm>
+
 #include "state.cuh"
 
 namespace idpd {
@@ -241,21 +243,59 @@ __global__ void __launch_bounds__(kRowBlock) k_scatter(DevState d, const int* ga
 }
 
 // Rows of one cell in ascending storage row: the order a stable counting
-// sort gives, independent of the arrival order of the atomics.
-__global__ void k_cell_sort(uint32_t* perm, const int* start, int ncell, const int* gate) {
-  if (gate && !*gate) return;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  const int b = start[c], e = start[c + 1];
-  for (int k = b + 1; k < e; k++) {
-    const uint32_t v = perm[k];
-    int m = k - 1;
-    while (m >= b && perm[m] > v) {
-      perm[m + 1] = perm[m];
-      m--;
+// sort gives, independent of the arrival order of the atomics. A warp per
+// cell: each of up to 128 rows finds its place by counting the smaller rows
+// (rows are distinct); a larger cell is sorted by one lane in place.
+__device__ __forceinline__ void sort_cell(uint32_t* perm, int b, int e, int lane) {
+  const int n = e - b;
+  if (n <= 1) return;
+  if (n <= 128) {
+    uint32_t v[4];
+    int rank[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      v[q] = 32 * q + lane < n ? perm[b + 32 * q + lane] : 0xFFFFFFFFu;
+      rank[q] = 0;
     }
-    perm[m + 1] = v;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (32 * q >= n) break;  // warp-uniform
+      for (int j = 0; j < 32; j++) {
+        const uint32_t x = __shfl_sync(0xffffffffu, v[q], j);
+#pragma unroll
+        for (int m = 0; m < 4; m++) rank[m] += x < v[m];
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (32 * q + lane < n) perm[b + rank[q]] = v[q];
+    __syncwarp();
+    return;
   }
+  if (lane == 0) {
+    for (int k = b + 1; k < e; k++) {
+      const uint32_t v = perm[k];
+      int m = k - 1;
+      while (m >= b && perm[m] > v) {
+        perm[m + 1] = perm[m];
+        m--;
+      }
+      perm[m + 1] = v;
+    }
+  }
+  __syncwarp();
+}
+
+constexpr int kSortWarps = 8;
+constexpr int kSortBlocks = 1216;  // 8 per SM of a GB300; the cells are strided over them
+
+__global__ void __launch_bounds__(32 * kSortWarps) k_cell_sort(uint32_t* perm, const int* start,
+                                                               int ncell, const int* gate) {
+  if (gate && !*gate) return;
+  const int lane = threadIdx.x & 31;
+  for (int c = blockIdx.x * kSortWarps + (threadIdx.x >> 5); c < ncell; c += gridDim.x * kSortWarps)
+    sort_cell(perm, start[c], start[c + 1], lane);
 }
 
 // Offset of x from its frame cell's origin o, at the periodic image nearest
@@ -310,7 +350,9 @@ void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cuda
 }
 
 void launch_cell_sort_raw(uint32_t* perm, const int* start, int ncell, cudaStream_t st) {
-  if (ncell > 0) k_cell_sort<<<(ncell + 255) / 256, 256, 0, st>>>(perm, start, ncell, nullptr);
+  if (ncell > 0)
+    k_cell_sort<<<std::min((ncell + kSortWarps - 1) / kSortWarps, kSortBlocks), 32 * kSortWarps,
+                  0, st>>>(perm, start, ncell, nullptr);
 }
 
 // Cell index and arrival slot of rows given as x y z triples (one grid, no
@@ -358,7 +400,8 @@ void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool s
   if (nblk == 0) return;
   k_scatter<<<nblk, kRowBlock, 0, st>>>(d, gate);
   if (stable)
-    k_cell_sort<<<(ncell_tot + 255) / 256, 256, 0, st>>>(d.perm, d.cell_start, ncell_tot, gate);
+    k_cell_sort<<<std::min((ncell_tot + kSortWarps - 1) / kSortWarps, kSortBlocks),
+                  32 * kSortWarps, 0, st>>>(d.perm, d.cell_start, ncell_tot, gate);
   k_pack<<<nblk, kRowBlock, 0, st>>>(d, gate);
 }
 
