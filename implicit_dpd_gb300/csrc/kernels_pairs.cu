@@ -405,8 +405,9 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
       __syncwarp();
       P[lane] = lane < nb ? d.posf[me] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       __syncwarp();
-      uint32_t* out = d.vl + (size_t)me * kVerletCap;
+      uint32_t* out = d.vl + (size_t)me * kVerletCap;  // 16-byte aligned rows
       int cnt = 0;
+      uint32_t w0 = 0, w1 = 0, w2 = 0;
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {
         const int tb = S.tb[g], te = S.te[g];
@@ -442,12 +443,26 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
           const unsigned self = (unsigned)(me - t0);  // the particle itself is no candidate
           if (self < 32u && me < te) mine &= ~(1u << self);
           __syncwarp();
-          while (mine) {
+          while (mine) {  // four entries gathered per 16-byte store
             const int j = __ffs(mine) - 1;
             mine &= mine - 1;
-            if (cnt < kVerletCap) out[cnt] = E[j];
+            const uint32_t v = E[j];
+            const int slot = cnt & 3;
+            w0 = slot == 0 ? v : w0;
+            w1 = slot == 1 ? v : w1;
+            w2 = slot == 2 ? v : w2;
+            if (slot == 3 && cnt < kVerletCap)
+              *reinterpret_cast<uint4*>(out + cnt - 3) = make_uint4(w0, w1, w2, v);
             cnt++;
           }
+        }
+      }
+      if (lane < nb) {  // the last entries short of four
+        const int slot = cnt & 3, base = cnt - slot;
+        if (base < kVerletCap) {
+          if (slot > 0) out[base] = w0;
+          if (slot > 1) out[base + 1] = w1;
+          if (slot > 2) out[base + 2] = w2;
         }
       }
       if (lane < nb) {
