@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
 // stencil of neighbour segments and, per candidate, the frame offset, so a
 // warp takes one cell at a time and up to 32 of its particles at once: each
 // lane loads one candidate, every particle of the batch is tested against
-// the 32 candidates (one ballot per particle), and each lane then appends
-// the candidates in range of its own particle to that particle's list. A
+// the 32 candidates (one ballot per particle), and the lanes whose candidate
+// is in range append it to that particle's list in one coalesced store. A
 // candidate is kept when closer than 1 + skin in FP32 (with a margin: the
 // list only has to hold every pair that can come within the cutoff before
 // the next rebuild). The warp of a 32-row chunk takes the cells whose first
@@ -374,14 +374,13 @@ template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ float4 bpos[kWarps][32];
-  __shared__ uint32_t ent[kWarps][32];
   if (!d.vdev->rebuild) return;
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
   float4* P = bpos[wid];
-  uint32_t* E = ent[wid];
+  const uint32_t lt_mask = (1u << lane) - 1u;
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const float rv2 = d.vdev->rv2;
@@ -405,9 +404,7 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
       __syncwarp();
       P[lane] = lane < nb ? d.posf[me] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       __syncwarp();
-      uint32_t* out = d.vl + (size_t)me * kVerletCap;  // 16-byte aligned rows
-      int cnt = 0;
-      uint32_t w0 = 0, w1 = 0, w2 = 0;
+      int cnt = 0;  // the list length of the lane's particle
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {
         const int tb = S.tb[g], te = S.te[g];
@@ -430,39 +427,19 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
             qz = fmaf((float)dz, csz, pj.z);
             e = make_entry(t, fx, dy, dz);
           }
-          __syncwarp();
-          E[lane] = e;
-          uint32_t mine = 0;  // candidates in range of the lane's particle
+          // per particle k of the batch: the lanes whose candidate is in range
+          // write it to k's list, consecutive lanes to consecutive slots
 #pragma unroll 4
           for (int k = 0; k < nb; k++) {
             const float4 pk = P[k];
             const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
-            const uint32_t m = __ballot_sync(0xffffffffu, ex * ex + ey * ey + ez * ez < rv2);
-            mine = lane == k ? m : mine;
+            const bool in = ex * ex + ey * ey + ez * ez < rv2 && t != b0 + k;
+            const uint32_t m = __ballot_sync(0xffffffffu, in);
+            const int base = __shfl_sync(0xffffffffu, cnt, k);
+            const int pos = base + __popc(m & lt_mask);
+            if (in && pos < kVerletCap) d.vl[(size_t)(b0 + k) * kVerletCap + pos] = e;
+            if (lane == k) cnt += __popc(m);
           }
-          const unsigned self = (unsigned)(me - t0);  // the particle itself is no candidate
-          if (self < 32u && me < te) mine &= ~(1u << self);
-          __syncwarp();
-          while (mine) {  // four entries gathered per 16-byte store
-            const int j = __ffs(mine) - 1;
-            mine &= mine - 1;
-            const uint32_t v = E[j];
-            const int slot = cnt & 3;
-            w0 = slot == 0 ? v : w0;
-            w1 = slot == 1 ? v : w1;
-            w2 = slot == 2 ? v : w2;
-            if (slot == 3 && cnt < kVerletCap)
-              *reinterpret_cast<uint4*>(out + cnt - 3) = make_uint4(w0, w1, w2, v);
-            cnt++;
-          }
-        }
-      }
-      if (lane < nb) {  // the last entries short of four
-        const int slot = cnt & 3, base = cnt - slot;
-        if (base < kVerletCap) {
-          if (slot > 0) out[base] = w0;
-          if (slot > 1) out[base + 1] = w1;
-          if (slot > 2) out[base + 2] = w2;
         }
       }
       if (lane < nb) {
