@@ -360,6 +360,65 @@ def reaction_bench(tune, steps=100, equil=2000, device=0):
                            "tail bead (Saru(id, step, seed) draw, bit-exact decisions)"}
 
 
+def liquid_bench(steps=200, equil=300, device=0):
+    """The 10^6-particle MDPD liquid: 55^3 box at density 6 (998,250
+    particles), Warren form A = -40, B = 25, r_d = 0.75, sigma 3, dt 0.005,
+    uniform random start. The FP32 engine (tuned over reach and skin) against
+    the plain FP64 kernels of the same step, with the measured force error."""
+    from implicit_dpd_gb300.abi import CFG_FP64_PAIRS, FORM_WARREN
+    from implicit_dpd_gb300.engine import Engine, derive_params
+
+    box = np.array([55.0, 55.0, 55.0])
+    st = configs.liquid(box, 6.0, seed=12350)
+    n = len(st["pos"])
+    p = derive_params(configs.run_param(box, dt=0.005, cf_r=3.0))
+    p.seed, p.time, p.form = 2468, 1, FORM_WARREN
+    p.warren_a, p.warren_b, p.warren_rd = -40.0, 25.0, 0.75
+
+    def engine(flags=0, state=st):
+        e = Engine(flags=flags, sort_period=100, device=device)
+        e.set_params(p)
+        e.upload(state)
+        return e
+
+    e = engine()
+    e.step(equil)
+    times = {}
+    for reach, skin in [(1, 0.0), (1, 0.15), (1, 0.2), (1, 0.3)]:
+        e.set_tuning(reach, skin)
+        e.step(2)
+        e.step(30)
+        times[(reach, skin)] = e.last_step_ms() / 30
+    reach, skin = min(times, key=times.get)
+    e.set_tuning(reach, skin)
+    e.step(3)
+    e.step(steps)
+    v32 = n * steps / (e.last_step_ms() * 1e-3)
+    eq = e.download()
+    e.close()
+    st_eq = dict(st, pos=eq["pos"], vel=eq["vel"], acc=eq["acc"])
+    e32, e64 = engine(state=st_eq), engine(CFG_FP64_PAIRS, st_eq)
+    for x in (e32, e64):
+        x.density()
+        x.force()
+    f32, f64 = e32.download()["acc"], e64.download()["acc"]
+    e32.close()
+    mag = np.linalg.norm(f64, axis=1)
+    err = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, np.sqrt(np.mean(mag ** 2)))
+    e64.step(1)
+    e64.step(10)
+    v64 = n * 10 / (e64.last_step_ms() * 1e-3)
+    e64.close()
+    return {"workload": "mdpd_liquid_1m", "n_particles": int(n), "steps": steps,
+            "equilibration_steps": equil, "tuning": {"reach": reach, "skin": skin},
+            "value": v32, "fp64_plain": v64, "speedup_fp32_over_fp64": v32 / v64,
+            "unit": "particle-steps/s",
+            "force_error": {"max_rel": float(err.max()),
+                            "aggregate": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))},
+            "description": "55^3 periodic box at density 6, Warren form A -40, B 25, r_d 0.75, "
+                           "sigma 3, dt 0.005, uniform random start"}
+
+
 def replicas_bench(steps=20, n_rep=256, device=0):
     """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
     A in [-50, -30], B = 25, densities 5-7): all replicas in one handle,
@@ -590,6 +649,7 @@ def run_engine(args, rank, world, local_rank):
 
     batched = replicas_bench(device=local_rank) if not args.no_replicas else None
     reaction = reaction_bench(reach, device=local_rank) if not args.no_reaction else None
+    liquid = liquid_bench(device=local_rank) if not args.no_liquid else None
     cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
     n_reorders = args.steps // 100
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -602,7 +662,7 @@ def run_engine(args, rank, world, local_rank):
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
-           "batched_replicas": batched, "reaction": reaction,
+           "batched_replicas": batched, "reaction": reaction, "liquid": liquid,
            "gpu_launches": args.steps * (KERNELS_PER_KEPT_STEP if reach["skin"] > 0 else KERNELS_PER_STEP)
                            + n_reorders * KERNELS_PER_REORDER,
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
@@ -626,6 +686,8 @@ def main():
     ap.add_argument("--no-replicas", action="store_true")
     ap.add_argument("--no-reaction", action="store_true",
                     help="skip the membrane-with-precursor line")
+    ap.add_argument("--no-liquid", action="store_true",
+                    help="skip the 10^6-particle MDPD liquid line")
     ap.add_argument("--box", type=float, nargs=3, default=list(BOX),
                     help="periodic box of the stacked-bilayer workload")
     ap.add_argument("--layers", type=int, default=N_LAYERS, help="bilayers stacked along z")
