@@ -221,6 +221,20 @@ void fill_repdev(RepDev& R, const idpd_params& p, int reach, float skin) {
   R.dens_unscale_f = (float)R.dens_unscale;
 }
 
+// A caller buffer that lives in device or managed memory, which the kernels
+// read or write where it lies; null for host memory, which goes through the
+// staging buffer and a copy engine (page-locked memory read by the kernels
+// over the host link measured slower than the copies).
+const void* device_view(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  return nullptr;
+}
+
 // Bit f set when some replica uses pair-force form f.
 int form_mask(const idpd_handle* h) {
   int m = 0;
@@ -940,15 +954,23 @@ int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double
   const RepDev& R = h->reps_h[r];
   const size_t n = (size_t)R.n;
   if (n == 0) return IDPD_OK;
-  // three contiguous copies: pos, vel, acc one after the other
-  const size_t bytes = 3 * n * sizeof(double);
-  CK(cudaMemcpyAsync(h->xfer, pos, bytes, cudaMemcpyHostToDevice, h->st));
-  CK(cudaMemcpyAsync(h->xfer + 3 * n, vel, bytes, cudaMemcpyHostToDevice, h->st));
-  CK(cudaMemcpyAsync(h->xfer + 6 * n, acc, bytes, cudaMemcpyHostToDevice, h->st));
+  // device buffers are read by the kernel where they lie; host ones are
+  // copied to the staging buffer first
+  const double* src[3] = {pos, vel, acc};
+  const double* dev[3];
+  for (int k = 0; k < 3; k++) {
+    dev[k] = static_cast<const double*>(device_view(src[k]));
+    if (!dev[k]) {
+      double* stage = h->xfer + 3 * n * k;
+      CK(cudaMemcpyAsync(stage, src[k], 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      dev[k] = stage;
+    }
+  }
   // with built kept lists the position change counts as displacement (the
   // next step rebuilds when it is too large); else the lists are rebuilt
   const bool kept = h->d.vdev && !h->vl_dirty && h->tune.skin > 0.0f;
-  launch_set_dynamics(h->d, h->xfer, R.row_off, R.n, R.box[0], R.box[1], R.box[2], kept, h->st);
+  launch_set_dynamics(h->d, dev[0], dev[1], dev[2], R.row_off, R.n, R.box[0], R.box[1], R.box[2],
+                      kept, h->st);
   h->density_valid = false;
   return IDPD_OK;
 }
@@ -1019,10 +1041,14 @@ int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, dou
   struct F { const double *x, *y, *z; double* out; } f3[3] = {
       {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
   int rc = IDPD_OK;
-  for (int k = 0; k < 3; k++) {  // into the staging buffer, then one copy each
+  for (int k = 0; k < 3; k++) {
     if (!f3[k].out) continue;
-    double* tmp = h->xfer + 3 * (size_t)n * k;
-    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.orig, R.row_off, tmp, n, h->st);
+    // device buffers are written by the kernel directly; host ones through
+    // the staging buffer and one copy
+    double* view = static_cast<double*>(const_cast<void*>(device_view(f3[k].out)));
+    double* tmp = view ? view : h->xfer + 3 * (size_t)n * k;
+    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.loc, R.row_off, tmp, n, h->st);
+    if (view) continue;
     cudaError_t e = cudaMemcpyAsync(f3[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
     if (e != cudaSuccess) rc = fail(h, IDPD_ERR_CUDA, "download: %s", cudaGetErrorString(e));
   }

@@ -346,14 +346,15 @@ void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n
 // image, as displacement for the kept lists (the delta_sumr of their last
 // rebuild moves back by it), so a host that hands back the positions it read
 // keeps the lists, and one that moves particles far enough triggers a rebuild.
-__global__ void k_set_dynamics(DevState d, const double* xfer, int row0, int n, double b0,
-                               double b1, double b2, int kept) {
+__global__ void k_set_dynamics(DevState d, const double* pos, const double* vel,
+                               const double* acc, int row0, int n, double b0, double b1,
+                               double b2, int kept) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t i = d.loc[row0 + k];
-  const double* p = xfer + 3 * (size_t)k;
-  const double* v = xfer + 3 * ((size_t)n + k);
-  const double* a = xfer + 3 * (2 * (size_t)n + k);
+  const double* p = pos + 3 * (size_t)k;
+  const double* v = vel + 3 * (size_t)k;
+  const double* a = acc + 3 * (size_t)k;
   const double box[3] = {b0, b1, b2};
   bool ok = true;
 #pragma unroll
@@ -375,29 +376,31 @@ __global__ void k_set_dynamics(DevState d, const double* xfer, int row0, int n, 
   d.ax[i] = a[0]; d.ay[i] = a[1]; d.az[i] = a[2];
 }
 
-void launch_set_dynamics(const DevState& d, const double* xfer, int row0, int n, double box0,
-                         double box1, double box2, bool kept, cudaStream_t st) {
+void launch_set_dynamics(const DevState& d, const double* pos, const double* vel,
+                         const double* acc, int row0, int n, double box0, double box1,
+                         double box2, bool kept, cudaStream_t st) {
   if (n == 0) return;
-  k_set_dynamics<<<(n + 255) / 256, 256, 0, st>>>(d, xfer, row0, n, box0, box1, box2,
+  k_set_dynamics<<<(n + 255) / 256, 256, 0, st>>>(d, pos, vel, acc, row0, n, box0, box1, box2,
                                                   kept ? 1 : 0);
 }
 
-// Storage rows [row0, row0 + n) back to upload order: aos[orig - row0] = row.
+// Storage rows of one replica back to upload order, three doubles per row:
+// output row k comes from storage row loc[row0 + k], so the writes (to device
+// memory or straight to page-locked host memory) are in order.
 __global__ void k_soa_to_aos(const double* x, const double* y, const double* z,
-                             const uint32_t* orig, int row0, double* aos, int n) {
+                             const uint32_t* loc, int row0, double* aos, int n) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const int i = row0 + k;
-  const size_t o = (size_t)(orig[i] - (uint32_t)row0);
-  aos[3 * o] = x[i];
-  aos[3 * o + 1] = y[i];
-  aos[3 * o + 2] = z[i];
+  const uint32_t i = loc[row0 + k];
+  aos[3 * (size_t)k] = x[i];
+  aos[3 * (size_t)k + 1] = y[i];
+  aos[3 * (size_t)k + 2] = z[i];
 }
 
-void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* orig,
+void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* loc,
                        int row0, double* aos, int n, cudaStream_t st) {
   if (n == 0) return;
-  k_soa_to_aos<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, orig, row0, aos, n);
+  k_soa_to_aos<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, loc, row0, aos, n);
 }
 
 // ------------------------------------------------------------ observables

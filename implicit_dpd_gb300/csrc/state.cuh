@@ -231,9 +231,10 @@ void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* s
 void launch_saru_test(int n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3, int draws,
                       uint32_t* out_u, float* out_n, cudaStream_t st);
 void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n, cudaStream_t st);
-void launch_set_dynamics(const DevState& d, const double* xfer, int row0, int n, double box0,
-                         double box1, double box2, bool kept, cudaStream_t st);
-void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* orig,
+void launch_set_dynamics(const DevState& d, const double* pos, const double* vel,
+                         const double* acc, int row0, int n, double box0, double box1,
+                         double box2, bool kept, cudaStream_t st);
+void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* loc,
                        int row0, double* aos, int n, cudaStream_t st);
 
 }  // namespace idpd

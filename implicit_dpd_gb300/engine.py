@@ -110,7 +110,13 @@ def load(path=LIB_PATH):
 
 
 def _p(a):
-    return None if a is None else a.ctypes.data_as(C.c_void_p)
+    """Address of a numpy array, or of any buffer exposing data_ptr() (a torch
+    tensor, page-locked or on the device)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
 
 
 def last_error(h=None):
