@@ -419,11 +419,12 @@ def liquid_bench(steps=200, equil=300, device=0):
                            "sigma 3, dt 0.005, uniform random start"}
 
 
-def replicas_bench(steps=20, n_rep=256, device=0):
+def replicas_bench(steps=50, n_rep=256, device=0):
     """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
     A in [-50, -30], B = 25, densities 5-7): all replicas in one handle,
     one CUDA graph per step, against the same replicas stepped one handle at
-    a time. Returns particle-steps/s of both."""
+    a time with the same (reach, skin), tuned on the batch. Returns
+    particle-steps/s of both."""
     from implicit_dpd_gb300.abi import FORM_WARREN
     from implicit_dpd_gb300.engine import Engine, derive_params
 
@@ -440,6 +441,15 @@ def replicas_bench(steps=20, n_rep=256, device=0):
         eb.set_params(p, k)
         eb.upload(r["state"], k)
     eb.step(3)
+    times = {}
+    for reach, skin in [(1, 0.0), (1, 0.2), (1, 0.3)]:
+        eb.set_tuning(reach, skin)
+        eb.step(2)
+        eb.step(20)
+        times[(reach, skin)] = eb.last_step_ms()
+    reach, skin = min(times, key=times.get)
+    eb.set_tuning(reach, skin)
+    eb.step(3)
     eb.step(steps)
     batched = n_tot * steps / (eb.last_step_ms() * 1e-3)
     eb.close()
@@ -448,6 +458,7 @@ def replicas_bench(steps=20, n_rep=256, device=0):
         e = Engine(device=device)
         e.set_params(p)
         e.upload(r["state"])
+        e.set_tuning(reach, skin)
         e.step(3)
         singles.append(e)
     import torch
@@ -460,7 +471,8 @@ def replicas_bench(steps=20, n_rep=256, device=0):
     for e in singles:
         e.close()
     return {"workload": "mdpd_replicas_256", "n_replicas": n_rep, "n_particles": int(n_tot),
-            "steps": steps, "batched": batched, "one_at_a_time": one_at_a_time,
+            "steps": steps, "tuning": {"reach": reach, "skin": skin},
+            "batched": batched, "one_at_a_time": one_at_a_time,
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
             "description": "256 MDPD liquids (Warren form, A in [-50,-30], B 25, r_d 0.75, "
                            "densities 5-7, 2k-60k particles log-uniform) in one handle and one "
