@@ -374,12 +374,16 @@ template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ float4 bpos[kWarps][32];
+  __shared__ float4 qpos[kWarps][64];
+  __shared__ uint32_t qent[kWarps][64];
   if (!d.vdev->rebuild) return;
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
   float4* P = bpos[wid];
+  float4* QX = qpos[wid];
+  uint32_t* QE = qent[wid];
   const uint32_t lt_mask = (1u << lane) - 1u;
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
@@ -402,9 +406,40 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
       const int nb = min(32, ce - b0);
       const int me = b0 + lane;  // the lane's particle (lane < nb)
       __syncwarp();
-      P[lane] = lane < nb ? d.posf[me] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const float4 pm = lane < nb ? d.posf[me] : d.posf[b0];
+      P[lane] = pm;
+      // the batch's bounding box: a candidate farther than 1 + skin from it
+      // is no candidate of any particle of the batch (about a quarter of the
+      // 27-cell stencil)
+      float lox = pm.x, hix = pm.x, loy = pm.y, hiy = pm.y, loz = pm.z, hiz = pm.z;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+        hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+        loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+        hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+        loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+        hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+      }
       __syncwarp();
       int cnt = 0;  // the list length of the lane's particle
+      int qn = 0;   // candidates queued for the next full round
+      // tests the 32 queued candidates against every particle of the batch:
+      // the lanes whose candidate is in range of particle k write it to k's
+      // list, consecutive lanes to consecutive slots
+      auto round = [&](float qx, float qy, float qz, uint32_t e, int t) {
+#pragma unroll 4
+        for (int k = 0; k < nb; k++) {
+          const float4 pk = P[k];
+          const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
+          const bool in = ex * ex + ey * ey + ez * ez < rv2 && t != b0 + k;
+          const uint32_t m = __ballot_sync(0xffffffffu, in);
+          const int base = __shfl_sync(0xffffffffu, cnt, k);
+          const int pos = base + __popc(m & lt_mask);
+          if (in && pos < kVerletCap) d.vl[(size_t)(b0 + k) * kVerletCap + pos] = e;
+          if (lane == k) cnt += __popc(m);
+        }
+      };
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {
         const int tb = S.tb[g], te = S.te[g];
@@ -416,32 +451,55 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
         const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
         for (int t0 = tb; t0 < te; t0 += 32) {
           const int t = t0 + lane;
-          // the candidate in the frame of the cell's particles (far away when absent)
-          float qx = 1.0e30f, qy = 0.0f, qz = 0.0f;
+          bool keep = false;
+          float qx = 0.0f, qy = 0.0f, qz = 0.0f;
           uint32_t e = 0;
           if (t < te) {
+            // the candidate in the frame of the cell's particles
             const float4 pj = __ldg(d.posf + t);
             const int fx = fx0 + frame_step<REACH>(t, b);
             qx = fmaf((float)fx, csx, pj.x);
             qy = fmaf((float)dy, csy, pj.y);
             qz = fmaf((float)dz, csz, pj.z);
             e = make_entry(t, fx, dy, dz);
+            const float ox = fmaxf(fmaxf(lox - qx, qx - hix), 0.0f);
+            const float oy = fmaxf(fmaxf(loy - qy, qy - hiy), 0.0f);
+            const float oz = fmaxf(fmaxf(loz - qz, qz - hiz), 0.0f);
+            keep = ox * ox + oy * oy + oz * oz < rv2;
           }
-          // per particle k of the batch: the lanes whose candidate is in range
-          // write it to k's list, consecutive lanes to consecutive slots
-#pragma unroll 4
-          for (int k = 0; k < nb; k++) {
-            const float4 pk = P[k];
-            const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
-            const bool in = ex * ex + ey * ey + ez * ez < rv2 && t != b0 + k;
-            const uint32_t m = __ballot_sync(0xffffffffu, in);
-            const int base = __shfl_sync(0xffffffffu, cnt, k);
-            const int pos = base + __popc(m & lt_mask);
-            if (in && pos < kVerletCap) d.vl[(size_t)(b0 + k) * kVerletCap + pos] = e;
-            if (lane == k) cnt += __popc(m);
+          const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+          if (keep) {
+            const int at = qn + __popc(mask & lt_mask);
+            QX[at] = make_float4(qx, qy, qz, __int_as_float(t));
+            QE[at] = e;
+          }
+          qn += __popc(mask);
+          if (qn >= 32) {
+            __syncwarp();
+            const float4 q = QX[lane];
+            const uint32_t qe = QE[lane];
+            __syncwarp();
+            if (lane < qn - 32) {
+              QX[lane] = QX[32 + lane];
+              QE[lane] = QE[32 + lane];
+            }
+            __syncwarp();
+            qn -= 32;
+            round(q.x, q.y, q.z, qe, __float_as_int(q.w));
           }
         }
       }
+      __syncwarp();
+      if (qn > 0) {  // the last, partial round (absent lanes far away)
+        float4 q = make_float4(1.0e30f, 0.0f, 0.0f, __int_as_float(-1));
+        uint32_t qe = 0;
+        if (lane < qn) {
+          q = QX[lane];
+          qe = QE[lane];
+        }
+        round(q.x, q.y, q.z, qe, __float_as_int(q.w));
+      }
+      __syncwarp();
       if (lane < nb) {
         d.vn[me] = cnt <= kVerletCap ? (uint16_t)cnt : (uint16_t)kNbrFallback;
         const uint32_t i = d.perm[me];
