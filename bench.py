@@ -523,7 +523,8 @@ def pinned(shape):
     return t, t.numpy()
 
 
-TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2), (2, 0.3)]
+TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
+                (2, 0.3)]
 
 
 def autotune(e, steps=40):
