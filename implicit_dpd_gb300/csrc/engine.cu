@@ -18,7 +18,9 @@ using namespace idpd;
 
 namespace {
 
-std::string g_lib_err;
+// The message of the last failure without a handle, per host thread (calls
+// on different handles may run on different threads).
+thread_local std::string g_lib_err;
 
 struct Staged {  // one replica's rows as uploaded (upload order)
   std::vector<double> pos, vel, acc;

@@ -110,8 +110,9 @@ typedef struct idpd_config {
 
 int idpd_create(const idpd_config* cfg, idpd_handle** out);
 int idpd_destroy(idpd_handle* h);
-/* Copies the last error message of the handle (or of the library when h is
- * NULL) into buf, NUL terminated. */
+/* Copies the last error message of the handle (or, when h is NULL, of the
+ * last failed call without a handle on the calling thread) into buf, NUL
+ * terminated. */
 int idpd_last_error(const idpd_handle* h, char* buf, size_t len);
 
 /* Parameters of one replica (the Parameter statics + CalcForceEpEpDPD::m_seed). */
