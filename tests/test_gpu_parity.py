@@ -284,12 +284,14 @@ def test_cell_reach_gives_bit_identical_trajectories():
         assert np.array_equal(out[0][key], out[1][key]), key
 
 
-@pytest.mark.parametrize("rho", [30.0, 90.0])
+@pytest.mark.parametrize("rho", [30.0, 90.0, 160.0])
 def test_dense_membrane_density_force_match_oracle(rho):
     """The compacted membrane regime (~150 neighbours per bead at rho 30)
-    fills several 32-pair rounds per particle; at rho 90 the neighbour lists
-    overflow (> 256 entries, segments longer than 255 rows) and pass 2 walks
-    the cells again."""
+    fills several 32-pair rounds per particle; rho 90 (~380 pairs within the
+    cutoff) fills long lists; at rho 160 (~670 pairs, > 512) the pass-1 lists
+    overflow and pass 2 walks the cells again, and with a skin of 0.2 the
+    kept lists (~1,160 candidates, > 1,024) overflow too and pass 1 sweeps the
+    cells. Fine-grained passes, then one graph step with kept lists."""
     box = np.array([7.0, 7.0, 5.0]) if rho < 50 else np.array([5.0, 5.0, 5.0])
     rng = np.random.default_rng(12)
     st = configs.liquid(box, rho, seed=12, prop=1)
@@ -305,6 +307,17 @@ def test_dense_membrane_density_force_match_oracle(rho):
         e.force()
         worst, agg = rel_force_err(e.download()["acc"], acc)
         assert worst < FORCE_TOL, (reach, worst, agg)
+    e = engine_for(p, st)
+    e.set_tuning(1, 0.2)
+    s0 = e.download()
+    e.step(1)
+    s1 = e.download()
+    po = type(p).from_buffer_copy(p)
+    ref = {k: s0[k].copy() for k in ("pos", "vel", "acc", "id", "prop")}
+    O.md_step(po, ref, nthreads=4)
+    assert np.array_equal(s1["pos"], ref["pos"])
+    worst, agg = rel_force_err(s1["acc"], ref["acc"])
+    assert worst < FORCE_TOL, ("kept lists", worst, agg)
 
 
 def test_replicas_of_different_pair_forms_batched_equal_single():
