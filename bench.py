@@ -523,23 +523,13 @@ def pinned(shape):
     return t, t.numpy()
 
 
-TUNE_CHOICES = [(1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
-                (2, 0.3)]
-
-
 def autotune(e, steps=40):
     """Times each (cell reach, skin) on the current state over enough steps
-    to include list rebuilds, and keeps the fastest. The reach does not change
-    results; a skin changes them only by FP32 rounding (pair sets exact)."""
-    times = {}
-    for reach, skin in TUNE_CHOICES:
-        e.set_tuning(reach, skin)
-        e.step(2)
-        e.step(steps)
-        times[f"reach{reach}_skin{skin:g}"] = (e.last_step_ms() / steps, reach, skin)
-    best = min(times, key=lambda k: times[k][0])
-    e.set_tuning(times[best][1], times[best][2])
-    return {"reach": times[best][1], "skin": times[best][2]}, {k: v[0] for k, v in times.items()}
+    to include list rebuilds, and keeps the fastest (the package's tuner,
+    without its cache: the bench measures afresh)."""
+    from implicit_dpd_gb300.autotune import tune
+
+    return tune(e, steps=steps)
 
 
 def run_engine(args, rank, world, local_rank):

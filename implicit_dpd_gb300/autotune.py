@@ -1,0 +1,79 @@
+"""The engine's autotuner: picks the cell reach and the neighbour-list skin of
+a handle by timing each choice on the handle's current state, and caches the
+choice per GPU model and workload signature in a JSON file.
+
+Neither choice changes the pair sets (they are exact), and the fixed-point
+sums make the reach irrelevant to the results; a skin changes them only by
+the FP32 rounding of cell-local coordinates. So tuning is safe to run on the
+production state itself: the steps it times are ordinary steps.
+"""
+import json
+import math
+import os
+
+DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
+                   (2, 0.3))
+
+
+def default_cache_path():
+    """IDPD_TUNING_CACHE, else ~/.cache/implicit_dpd_gb300/tuning.json."""
+    env = os.environ.get("IDPD_TUNING_CACHE")
+    if env:
+        return env
+    return os.path.join(os.path.expanduser("~"), ".cache", "implicit_dpd_gb300", "tuning.json")
+
+
+def signature(gpu, n_particles, volume, form, n_replicas=1):
+    """Cache key: GPU model, pair-force form, replica count, particle count
+    and number density rounded to a quarter octave (systems that close tune
+    alike)."""
+    q = lambda x: round(4.0 * math.log2(max(x, 1e-12))) / 4.0
+    return f"{gpu}|form{form}|rep{n_replicas}|n2^{q(n_particles):g}|rho2^{q(n_particles / volume):g}"
+
+
+def _load(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(path, table):
+    d = os.path.dirname(path)
+    if d:
+        os.makedirs(d, exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, refresh=False):
+    """Applies the fastest (reach, skin) to `engine` and returns
+    (choice, times): times maps "reach{r}_skin{s}" to ms per step (empty when
+    the choice came from the cache). With a key and a cache path, a cached
+    choice is applied without timing unless refresh is set, and a new choice
+    is written back. Choices whose skin the box does not allow are skipped."""
+    table = _load(cache_path) if (cache_path and key) else {}
+    if key and not refresh and key in table:
+        reach, skin = table[key]["reach"], table[key]["skin"]
+        engine.set_tuning(reach, skin)
+        return {"reach": reach, "skin": skin}, {}
+    times = {}
+    for reach, skin in choices:
+        try:
+            engine.set_tuning(reach, skin)
+        except Exception:  # the box is too small for this skin
+            continue
+        engine.step(2)
+        engine.step(steps)
+        times[(reach, skin)] = engine.last_step_ms() / steps
+    if not times:
+        raise ValueError("no tuning choice fits this system")
+    reach, skin = min(times, key=times.get)
+    engine.set_tuning(reach, skin)
+    if cache_path and key:
+        table[key] = {"reach": reach, "skin": skin, "ms_per_step": times[(reach, skin)]}
+        _store(cache_path, table)
+    return {"reach": reach, "skin": skin}, {f"reach{r}_skin{s:g}": t for (r, s), t in times.items()}

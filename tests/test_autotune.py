@@ -1,0 +1,72 @@
+"""The autotuner's host logic (no GPU): choice of the fastest (reach, skin),
+skipping choices the box refuses, and the JSON cache per signature."""
+import json
+
+import pytest
+
+from implicit_dpd_gb300 import autotune as A
+
+
+class FakeEngine:
+    """Step times per (reach, skin); skins above max_skin are refused like a
+    box too small for them."""
+
+    def __init__(self, ms, max_skin=1.0):
+        self.ms, self.max_skin = ms, max_skin
+        self.tuning, self.steps, self.last = None, 0, 0.0
+
+    def set_tuning(self, reach, skin=0.0):
+        if skin > self.max_skin:
+            raise ValueError("skin needs a larger box")
+        self.tuning = (reach, skin)
+
+    def step(self, n):
+        self.steps += n
+        self.last = self.ms[self.tuning] * n
+
+    def last_step_ms(self):
+        return self.last
+
+
+def test_picks_the_fastest_and_applies_it():
+    ms = {c: 5.0 for c in A.DEFAULT_CHOICES}
+    ms[(1, 0.15)] = 3.2
+    e = FakeEngine(ms)
+    choice, times = A.tune(e)
+    assert choice == {"reach": 1, "skin": 0.15} and e.tuning == (1, 0.15)
+    assert times["reach1_skin0.15"] == pytest.approx(3.2)
+    assert len(times) == len(A.DEFAULT_CHOICES)
+
+
+def test_skips_choices_the_box_refuses():
+    ms = {c: 4.0 - c[1] for c in A.DEFAULT_CHOICES}  # larger skins faster
+    e = FakeEngine(ms, max_skin=0.15)
+    choice, times = A.tune(e)
+    assert choice["skin"] == 0.15
+    assert all(float(k.split("skin")[1]) <= 0.15 for k in times)
+    with pytest.raises(ValueError):
+        A.tune(FakeEngine(ms, max_skin=-1.0))
+
+
+def test_cache_round_trip(tmp_path):
+    path = str(tmp_path / "sub" / "tuning.json")
+    key = A.signature("GB300", 984040, 64 * 64 * 48, 0)
+    ms = {c: 5.0 for c in A.DEFAULT_CHOICES}
+    ms[(2, 0.2)] = 2.0
+    e = FakeEngine(ms)
+    A.tune(e, key=key, cache_path=path)
+    stored = json.load(open(path))
+    assert stored[key]["reach"] == 2 and stored[key]["skin"] == 0.2
+    e2 = FakeEngine(ms)
+    choice, times = A.tune(e2, key=key, cache_path=path)
+    assert choice == {"reach": 2, "skin": 0.2} and times == {} and e2.steps == 0
+    ms[(1, 0.1)] = 1.0
+    choice, times = A.tune(FakeEngine(ms), key=key, cache_path=path, refresh=True)
+    assert choice == {"reach": 1, "skin": 0.1} and json.load(open(path))[key]["skin"] == 0.1
+
+
+def test_signature_groups_close_systems():
+    a = A.signature("GB300", 1_000_000, 196_608, 0)
+    b = A.signature("GB300", 1_020_000, 200_000, 0)
+    c = A.signature("GB300", 2_000_000, 196_608, 0)
+    assert a == b and a != c and a != A.signature("GB300", 1_000_000, 196_608, 2)
