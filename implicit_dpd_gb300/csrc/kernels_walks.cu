@@ -192,7 +192,6 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_walk_force(WalkDev w, RepDe
   const int jb = w.j_off[walk], je = w.j_off[walk + 1];
   const float4 pi = w.pi[i], li = w.li[i], vi = w.vi[i], di = w.di[i];
   const uint32_t idi = __float_as_uint(vi.w), pri = __float_as_uint(pi.w);
-  const double* xi = w.xi + 3 * (size_t)i;
   long long f[6] = {0, 0, 0, 0, 0, 0};
   int* Q = queue[wid];
   int qn = 0;

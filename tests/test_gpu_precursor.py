@@ -57,24 +57,25 @@ def test_precursor_decisions_match_oracle(flags, skin):
 
 
 def test_precursor_through_an_overflowed_list():
-    """400 precursors packed within 0.8 of a tail bead: more than 256 pairs
-    within the cutoff, so pass 1 keeps no list for them and the conversion
-    sweeps the cells."""
+    """700 precursors packed within 0.8 of a tail bead: the tail bead and most
+    of the precursors have more than 512 pairs within the cutoff, so pass 1
+    keeps no list for them and the conversion sweeps the cells."""
     box, st, n_amp = mixed_system(seed=13)
+    NB = 700
     rng = np.random.default_rng(5)
     tail = int(np.flatnonzero(st["prop"] == HYPHOB)[0])
-    v = rng.normal(size=(400, 3))
-    v *= (0.8 * rng.random(400) ** (1 / 3) / np.linalg.norm(v, axis=1))[:, None]
+    v = rng.normal(size=(NB, 3))
+    v *= (0.8 * rng.random(NB) ** (1 / 3) / np.linalg.norm(v, axis=1))[:, None]
     blob = np.mod(st["pos"][tail] + v, box)
     n0 = len(st["pos"])
     st = dict(st)
     st["pos"] = np.concatenate([st["pos"], blob])
-    st["vel"] = np.concatenate([st["vel"], np.zeros((400, 3))])
-    st["acc"] = np.concatenate([st["acc"], np.zeros((400, 3))])
-    st["prop"] = np.concatenate([st["prop"], np.full(400, SOLVENT, np.uint32)])
+    st["vel"] = np.concatenate([st["vel"], np.zeros((NB, 3))])
+    st["acc"] = np.concatenate([st["acc"], np.zeros((NB, 3))])
+    st["prop"] = np.concatenate([st["prop"], np.full(NB, SOLVENT, np.uint32)])
     for k in ("amp_id", "unit"):
-        st[k] = np.concatenate([st[k], np.full(400, 0xFFFFFFFF, np.uint32)])
-    st["id"] = np.arange(n0 + 400, dtype=np.uint32)
+        st[k] = np.concatenate([st[k], np.full(NB, 0xFFFFFFFF, np.uint32)])
+    st["id"] = np.arange(n0 + NB, dtype=np.uint32)
     p = mdpd_params(box, time=31)
     thr = precursor_threshold(0.5)
     e = _engine(p, st, n_amp)
