@@ -287,7 +287,9 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.scan_part, (cc + 4095) / 4096 + 1);
   AL(d.perm, cap); AL(d.rank, cap); AL(d.scell, cap);
   AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap); AL(d.poslo, cap);
-  AL(d.fqx, cap); AL(d.fqy, cap); AL(d.fqz, cap);
+  AL(d.fqx, 3 * (size_t)cap);
+  d.fqy = d.fqx + cap;
+  d.fqz = d.fqx + 2 * (size_t)cap;
   AL(d.nbl, (size_t)kNbrCap * cap); AL(d.nbn, cap);
   AL(d.topol, 4 * ac);
   AL(d.cf_bend, ac);
@@ -318,9 +320,9 @@ int ensure_press(idpd_handle* h) {
   if (h->d.pqx) return IDPD_OK;
   int rc;
   DevState& d = h->d;
-  if ((rc = dalloc(h, &d.pqx, h->cap)) || (rc = dalloc(h, &d.pqy, h->cap)) ||
-      (rc = dalloc(h, &d.pqz, h->cap)))
-    return rc;
+  if ((rc = dalloc(h, &d.pqx, 3 * (size_t)h->cap))) return rc;
+  d.pqy = d.pqx + h->cap;
+  d.pqz = d.pqx + 2 * (size_t)h->cap;
   invalidate_graph(h);
   return IDPD_OK;
 }
@@ -668,10 +670,10 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
-  launch_force(d, h->nblk, fp64, observe, h->tune, form_mask(h), h->st);
+  launch_force(d, h->nblk, fp64, observe, h->tune, form_mask(h), h->cap, h->st);
   if (h->prec_any) {
     d.prec_count = h->prec_dev;
-    launch_precursor(d, h->nblk, !fp64, h->st);
+    launch_precursor(d, h->nblk, verlet, h->st);
   }
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
@@ -1169,7 +1171,7 @@ int idpd_force(idpd_handle* h) {
   if (!h->density_valid) return fail(h, IDPD_ERR_STATE, "idpd_force needs idpd_density on the same positions");
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
-  launch_force(h->d, h->nblk, fp64, true, h->tune, form_mask(h), h->st);
+  launch_force(h->d, h->nblk, fp64, true, h->tune, form_mask(h), h->cap, h->st);
   launch_fq_to_acc(h->d, h->nblk, h->press64, h->st);
   return check_device_error(h);
 }
@@ -1368,7 +1370,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[4], h->st));
   launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_force(d, h->nblk, fp64, false, h->tune, form_mask(h), h->st);
+  launch_force(d, h->nblk, fp64, false, h->tune, form_mask(h), h->cap, h->st);
   CK(cudaEventRecord(ev[6], h->st));
   launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[7], h->st));

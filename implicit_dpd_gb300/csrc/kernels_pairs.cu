@@ -133,10 +133,23 @@ __device__ __forceinline__ PairCode unpack_code(uint32_t c) {
 // Neighbour list entry (32 bits): the candidate's sorted row (25 bits) and
 // its frame cell's offset from the particle's frame cell, dx, dy, dz + 1 in
 // 2 bits each. kNbrFallback marks a particle whose list did not fit (the
-// next pass walks its cells again).
+// next pass walks its cells again). A pass-1 list holds the pairs within the
+// cutoff that the particle owns (owns()).
 constexpr uint32_t kNbrFallback = 0xffffu;
 constexpr int kRowBits = 25;
 constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
+
+// Pass 2 evaluates each pair once, from the side of the particle that owns
+// it: the frame offset dx of the other particle decides when nonzero, else
+// (the same frame cell column) the larger cell-local x of the step, else the
+// larger sorted row. Every path of a step decides on the same FP32 rows, so
+// the two particles of a pair always agree, and each particle owns about
+// half of its pairs (those on the +x side of the plane through it), which
+// keeps the two particles of a half-warp pair in pass 2 near equal work.
+__device__ __forceinline__ bool owns(int dx, float xj, float xi, int t, int s) {
+  if (dx != 0) return dx > 0;
+  return xj != xi ? xj > xi : t > s;
+}
 
 __device__ __forceinline__ uint32_t make_entry(int t, int dx, int dy, int dz) {
   return (uint32_t)t | ((uint32_t)(dx + 1) << kRowBits) | ((uint32_t)(dy + 1) << (kRowBits + 2)) |
@@ -172,7 +185,8 @@ __device__ __forceinline__ void add_weight(uint32_t& q0, uint32_t& q1, uint32_t&
 // list with every lane busy and copies the list out for pass 2 (a particle
 // whose list overflows takes its weights during a second sweep). With kept
 // lists (VERLET): one pass over the particle's kept list tests each
-// candidate, adds its weight and appends it to the list of pass 2.
+// candidate, adds its weight and appends it to the list of pass 2 when the
+// particle owns the pair.
 template <int REACH, bool VERLET>
 __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
@@ -195,7 +209,9 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
   for (int s = s0; s < s_end; s++) {
     const float4 pi = d.posf[s];
     const uint32_t si = d.perm[s];
-    int nl = 0;
+    int nl = 0, nu = 0;  // pairs within the cutoff, owned ones among them
+    int nw = 0;          // bound on the weighted pairs
+    bool swept = true;   // the pairs came from a sweep of the cells (list out below)
     uint32_t q0 = 0, q1 = 0, q2 = 0;
     // weight of one candidate; called by every lane together (valid = false
     // for lanes without one) so that the rare FP64 recheck is warp-uniform.
@@ -226,6 +242,7 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
     bool fits = true;
     if (VERLET && nv != kNbrFallback) {
       // ---- the particle's kept list: test, weight and list out in one pass
+      swept = false;
       const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
       uint32_t* out = d.nbl + (size_t)s * kNbrCap;
       uint32_t e_next = lane < (int)nv ? vl[lane] : 0u;  // one round ahead
@@ -237,15 +254,18 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
         int t, dx, dy, dz;
         read_entry(e, t, dx, dy, dz);
         if (!valid) t = s;
-        const bool in1 = test(valid, t, dx, dy, dz, __ldg(d.posf + t), false);
-        const uint32_t mask = __ballot_sync(0xffffffffu, in1);
-        if (in1) {
-          const int pos = nl + __popc(mask & lt_mask);
+        const float4 pj = __ldg(d.posf + t);
+        const bool in1 = test(valid, t, dx, dy, dz, pj, false);
+        const bool put = in1 && owns(dx, pj.x, pi.x, t, s);
+        const uint32_t mo = __ballot_sync(0xffffffffu, put);
+        if (put) {
+          const int pos = nu + __popc(mo & lt_mask);
           if (pos < kNbrCap) out[pos] = e;
         }
-        nl += __popc(mask);
+        nu += __popc(mo);
       }
-      fits = nl <= kNbrCap;
+      nw = (int)nv;
+      fits = nu <= kNbrCap;
     } else {
       const int cell = (int)d.scell[s];
       if (cell != cached) {
@@ -293,6 +313,7 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
       }
       __syncwarp();
       fits = nl <= kNbrCap;
+      nw = nl;
       // ---- phase B: density weights
       if (fits) {
         for (int k0 = 0; k0 < nl; k0 += 32) {
@@ -324,14 +345,27 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
       }
     }
     __syncwarp();
-    if (!VERLET && fits) {  // list out for pass 2, coalesced
+    if (swept && fits) {  // list out for pass 2: the owned pairs, coalesced
       uint32_t* out = d.nbl + (size_t)s * kNbrCap;
-      for (int k = lane; k < nl; k += 32) out[k] = L[k];
+      for (int k0 = 0; k0 < nl; k0 += 32) {
+        const int k = k0 + lane;
+        uint32_t e = 0u;
+        bool own = false;
+        if (k < nl) {
+          e = L[k];
+          int t, dx, dy, dz;
+          read_entry(e, t, dx, dy, dz);
+          own = owns(dx, __ldg(&d.posf[t].x), pi.x, t, s);
+        }
+        const uint32_t mo = __ballot_sync(0xffffffffu, own);
+        if (own) out[nu + __popc(mo & lt_mask)] = e;
+        nu += __popc(mo);
+      }
     }
-    // each weight is below 2^23, so up to 512 weighted pairs (every list:
-    // kept lists hold <= 512 candidates, pass-1 lists 256) total below 2^32
+    // each weight is below 2^23, so up to 512 weighted pairs total below
+    // 2^32 (nw bounds them: the kept list's length, or the pairs in range)
     unsigned long long a0, a1, a2;
-    if (nl <= 512) {
+    if (nw <= 512) {
       a0 = __reduce_add_sync(0xffffffffu, q0);
       a1 = __reduce_add_sync(0xffffffffu, q1);
       a2 = __reduce_add_sync(0xffffffffu, q2);
@@ -348,7 +382,7 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
       const float u = R->dens_unscale_f;
       d.densf[s] = make_float4(fix_to_float((long long)a0, u), fix_to_float((long long)a1, u),
                                fix_to_float((long long)a2, u), 0.0f);
-      d.nbn[s] = fits ? (uint16_t)nl : (uint16_t)kNbrFallback;
+      d.nbn[s] = fits ? (uint16_t)nu : (uint16_t)kNbrFallback;
       if (d.dqx) {
         d.dqx[s] = (long long)a0;
         d.dqy[s] = (long long)a1;
@@ -657,7 +691,7 @@ __device__ __forceinline__ void close_pair_vector(float4 pi, float4 li, float4 p
 // Pairs closer than 0.1 take their pair vector from close_pair_vector.
 constexpr float kCloseCut2 = 0.01f;
 
-// The particle of one warp in pass 2 and its fixed-point sums.
+// The particle of one (half) warp in pass 2 and its fixed-point sums.
 struct PairI {
   float4 pi, vi, di;
   uint32_t idi, pri, seed;
@@ -666,9 +700,18 @@ struct PairI {
   long long fx, fy, fz, px, py, pz;
 };
 
+__device__ __forceinline__ void load_row(PairI& I, const DevState& d, int s) {
+  I.pi = d.posf[s];
+  I.vi = d.velf[s];
+  I.di = d.densf[s];
+  I.row = s;
+  I.idi = fbits(I.vi.w);
+  I.pri = fbits(I.pi.w);
+}
+
 // A lane's share of one fixed-point sum of pass 2 as the sums of the
-// fix_force_parts of its terms. A list gives a lane at most kNbrCap / 32
-// terms, so the parts' warp totals stay below 2^30 and reduce in 32 bits.
+// fix_force_parts of its terms. A list holds at most kNbrCap terms, so the
+// parts' totals over a half warp stay below 2^30 and reduce in 32 bits.
 struct FixSum {
   int hi, lo;
   __device__ __forceinline__ void add(float v, bool& range) {
@@ -678,21 +721,27 @@ struct FixSum {
     hi += h;
     lo += l;
   }
-  __device__ __forceinline__ long long total() const {
-    return ((long long)__reduce_add_sync(0xffffffffu, hi) << 21) +
-           (long long)__reduce_add_sync(0xffffffffu, lo);
+  // the total over the lanes of half warp h (lanes 16 h .. 16 h + 15)
+  __device__ __forceinline__ long long half_total(int h) const {
+    const int hi0 = __reduce_add_sync(0xffffffffu, h ? 0 : hi);
+    const int hi1 = __reduce_add_sync(0xffffffffu, h ? hi : 0);
+    const int lo0 = __reduce_add_sync(0xffffffffu, h ? 0 : lo);
+    const int lo1 = __reduce_add_sync(0xffffffffu, h ? lo : 0);
+    return ((long long)(h ? hi1 : hi0) << 21) + (long long)(h ? lo1 : lo0);
   }
 };
-static_assert((kNbrCap / 32) * (1 << 21) < (1 << 26), "32-bit warp totals of the fixed-point parts");
+static_assert((long long)kNbrCap * (1 << 21) <= (1ll << 30), "32-bit totals of the fixed-point parts");
 
-// The force and virial terms of one pair (the pair arithmetic of pass 2).
+// The force and virial terms of one pair (the pair arithmetic of pass 2),
+// from the side of the particle that owns the pair (a pair of equal ids is
+// skipped, nbdf_calculator.hpp:84).
 template <bool PRESS, bool CHECK, int FORM>
 __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, const PairTables& T,
                                            const PairI& I, int t, int dx, int dy, int dz,
                                            float g[6]) {
   const float4 vj = __ldg(d.velf + t);
   const uint32_t idj = fbits(vj.w);
-  if (idj == I.idi) return false;  // nbdf_calculator.hpp:84
+  if (idj == I.idi) return false;
   const float4 pj = __ldg(d.posf + t);
   const float4 dj = __ldg(d.densf + t);
   float ex = (I.pi.x - (float)dx * I.csx) - pj.x;
@@ -726,19 +775,41 @@ __device__ __forceinline__ bool pair_terms(const DevState& d, const RepDev* R, c
   return true;
 }
 
-// One pair term added to the particle's sums in 32-bit parts.
+__device__ __forceinline__ void red_add(long long* p, long long v) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+}
+
+// The other particle's share of one pair term: the force -g (the exact
+// negation of the owner's fixed-point term) and the virial +g e.
+template <bool PRESS>
+__device__ __forceinline__ void add_to_other(const DevState& d, int t, const float g[6]) {
+  red_add(d.fqx + t, -fix_force(g[0]));
+  red_add(d.fqy + t, -fix_force(g[1]));
+  red_add(d.fqz + t, -fix_force(g[2]));
+  if (PRESS) {
+    red_add(d.pqx + t, fix_force(g[3]));
+    red_add(d.pqy + t, fix_force(g[4]));
+    red_add(d.pqz + t, fix_force(g[5]));
+  }
+}
+
+// One owned pair: the owner's term added to its sums in 32-bit parts, the
+// other particle's term to its fixed-point sums in memory.
 template <bool PRESS, int FORM>
-__device__ __forceinline__ void eval_pair_parts(const DevState& d, const RepDev* R,
-                                                const PairTables& T, const PairI& I, int t, int dx,
-                                                int dy, int dz, FixSum f[6], bool& range) {
+__device__ __forceinline__ void eval_owned_parts(const DevState& d, const RepDev* R,
+                                                 const PairTables& T, const PairI& I, int t,
+                                                 int dx, int dy, int dz, FixSum f[6],
+                                                 bool& range) {
   float g[6];
   if (!pair_terms<PRESS, false, FORM>(d, R, T, I, t, dx, dy, dz, g)) return;
 #pragma unroll
   for (int c = 0; c < (PRESS ? 6 : 3); c++) f[c].add(g[c], range);
+  add_to_other<PRESS>(d, t, g);
 }
 
-// One pair term added to the particle's sums (the lane's share).
-template <bool PRESS, int FORM>
+// One owned pair added to the owner's 64-bit sums (the lane's share) and,
+// with OTHER, to the other particle's sums in memory.
+template <bool PRESS, int FORM, bool OTHER>
 __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, const PairTables& T,
                                           PairI& I, int t, int dx, int dy, int dz) {
   float g[6];
@@ -751,12 +822,20 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
     I.py += fix_force(g[4]);
     I.pz += fix_force(g[5]);
   }
+  if (OTHER) add_to_other<PRESS>(d, t, g);
 }
 
-// One warp per particle. The list of pass 1 gives the pairs, 32 per round
-// with every lane busy; a particle whose list overflowed walks its cells
-// again and queues the in-range pairs in shared memory. One launch per pair
-// form present: a block whose replica has another form returns at once.
+// Each pair is evaluated once, by the particle that owns it (owns()), and
+// its term goes to both particles (Newton's third law in exact fixed point: the
+// sums equal those of the reference's two evaluations up to the FP32
+// rounding of one of them). A warp takes two particles at a time, 16 lanes
+// each, over the owned pairs at the front of their pass-1 lists; the sums
+// start at zero (launch_force) and every term arrives by atomic add. A
+// particle whose list overflowed walks its cells again with the whole warp
+// and queues the in-range pairs in shared memory; a particle with a term
+// outside the 32-bit parts' range is summed again in 64 bits (its own side
+// only). One launch per pair form present: a block whose replica has another
+// form returns at once.
 template <int REACH, bool PRESS, int FORM>
 __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
@@ -768,6 +847,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   if (threadIdx.x < 9) fill_pair_table(T, *R, threadIdx.x);
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int h = lane >> 4, sl = lane & 15;
   SegTable& S = seg[wid];
   uint32_t* QT = qt[wid];
   uint32_t* QC = qc[wid];
@@ -781,138 +861,145 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
   constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
-  for (int s = s0; s < s_end; s++) {
-    I.pi = d.posf[s];
-    I.vi = d.velf[s];
-    I.di = d.densf[s];
-    I.row = s;
-    I.idi = fbits(I.vi.w);
-    I.pri = fbits(I.pi.w);
-    const uint32_t cnt = d.nbn[s];
+  for (int s2 = s0; s2 < s_end; s2 += 2) {
+    // ---- two particles, 16 lanes each: the owned pairs of the lists
+    const bool act = s2 + h < s_end;
+    const int s = act ? s2 + h : s2;
+    load_row(I, d, s);
+    const uint32_t cnt = act ? (uint32_t)d.nbn[s] : 0u;
+    const int nu = cnt != kNbrFallback ? (int)cnt : 0;
     const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
-    if (cnt != kNbrFallback) {  // the list: sums in 32-bit parts
-      FixSum f[6];
+    FixSum f[6];
 #pragma unroll
-      for (int c = 0; c < 6; c++) f[c].hi = f[c].lo = 0;
-      bool range = true;
-      uint32_t e_next = lane < (int)cnt ? list[lane] : 0u;  // one round ahead
-      for (int k = lane; k < (int)cnt; k += 32) {
-        const uint32_t e = e_next;
-        if (k + 32 < (int)cnt) e_next = list[k + 32];
-        int t, dx, dy, dz;
-        read_entry(e, t, dx, dy, dz);
-        eval_pair_parts<PRESS, FORM>(d, R, T, I, t, dx, dy, dz, f, range);
-      }
-      if (__all_sync(0xffffffffu, range)) {
-        const long long fx = f[0].total(), fy = f[1].total(), fz = f[2].total();
-        long long px = 0, py = 0, pz = 0;
-        if (PRESS) {
-          px = f[3].total();
-          py = f[4].total();
-          pz = f[5].total();
-        }
-        if (lane == 0) {
-          d.fqx[s] = fx;
-          d.fqy[s] = fy;
-          d.fqz[s] = fz;
-          if (PRESS) {
-            d.pqx[s] = px;
-            d.pqy[s] = py;
-            d.pqz[s] = pz;
-          }
-        }
-        continue;
-      }
+    for (int c = 0; c < 6; c++) f[c].hi = f[c].lo = 0;
+    bool range = true;
+    for (int k = sl; k < nu; k += 16) {
+      int t, dx, dy, dz;
+      read_entry(list[k], t, dx, dy, dz);
+      eval_owned_parts<PRESS, FORM>(d, R, T, I, t, dx, dy, dz, f, range);
     }
-    // a term outside the 32-bit parts' range, or a list that did not fit:
-    // 64-bit sums
-    I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
-    if (cnt != kNbrFallback) {
-      for (int k = lane; k < (int)cnt; k += 32) {
-        int t, dx, dy, dz;
-        read_entry(list[k], t, dx, dy, dz);
-        eval_pair<PRESS, FORM>(d, R, T, I, t, dx, dy, dz);
-      }
-    } else {
-      const int cell = (int)d.scell[s];
-      if (cell != cached) {  // the segments of the particle's cell (only this path walks cells)
-        int cx, cy, cz;
-        cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
-        __syncwarp();
-        build_segments(S, d, R, cx, cy, cz, lane);
-        __syncwarp();
-        cached = cell;
-      }
-      int qn = 0;
-#pragma unroll 1
-      for (int g = 0; g < nseg; g++) {
-        const int tb = S.tb[g], te = S.te[g];
-        if (tb >= te) continue;
-        const int code = S.code[g];
-        int b[2 * REACH];
-#pragma unroll
-        for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
-        const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
-        const float by = I.pi.y - (float)dy * I.csy, bz = I.pi.z - (float)dz * I.csz;
-        for (int t0 = tb; t0 < te; t0 += 32) {
-          const int t = t0 + lane;
-          bool in = false;
-          int dx = 0;
-          bool near = false;
-          if (t < te && t != s) {
-            const float4 pj = __ldg(d.posf + t);
-            dx = fx0 + frame_step<REACH>(t, b);
-            const float ex = (I.pi.x - (float)dx * I.csx) - pj.x, ey = by - pj.y, ez = bz - pj.z;
-            const float dr2 = ex * ex + ey * ey + ez * ez;
-            in = dr2 < 1.0f;
-            near = fabsf(dr2 - 1.0f) <= kGuard;
-          }
-          if (__any_sync(0xffffffffu, near) && near) {
-            in = exact_dr2(d, R, d.perm[s], d.perm[t]) < 1.0;
-          }
-          const uint32_t mask = __ballot_sync(0xffffffffu, in);
-          if (in) {
-            const int pos = qn + __popc(mask & lt_mask);
-            QT[pos] = (uint32_t)t;
-            QC[pos] = pack_code(dx, code);
-          }
-          qn += __popc(mask);
-          if (qn >= 32) {
-            __syncwarp();
-            const PairCode pc = unpack_code(QC[lane]);
-            eval_pair<PRESS, FORM>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
-            __syncwarp();
-            if (lane < qn - 32) {
-              QT[lane] = QT[32 + lane];
-              QC[lane] = QC[32 + lane];
-            }
-            __syncwarp();
-            qn -= 32;
-          }
-        }
-      }
-      __syncwarp();
-      if (lane < qn) {
-        const PairCode pc = unpack_code(QC[lane]);
-        eval_pair<PRESS, FORM>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
-      }
-      __syncwarp();
-    }
-    const long long fx = warp_sum_ll(I.fx), fy = warp_sum_ll(I.fy), fz = warp_sum_ll(I.fz);
-    long long px = 0, py = 0, pz = 0;
-    if (PRESS) {
-      px = warp_sum_ll(I.px);
-      py = warp_sum_ll(I.py);
-      pz = warp_sum_ll(I.pz);
-    }
-    if (lane == 0) {
-      d.fqx[s] = fx;
-      d.fqy[s] = fy;
-      d.fqz[s] = fz;
+    __syncwarp();
+    const uint32_t bad = __ballot_sync(0xffffffffu, !range);
+    const bool ok = ((bad >> (16 * h)) & 0xffffu) == 0u;
+    {
+      const long long fx = f[0].half_total(h), fy = f[1].half_total(h), fz = f[2].half_total(h);
+      long long px = 0, py = 0, pz = 0;
       if (PRESS) {
-        d.pqx[s] = px;
-        d.pqy[s] = py;
-        d.pqz[s] = pz;
+        px = f[3].half_total(h);
+        py = f[4].half_total(h);
+        pz = f[5].half_total(h);
+      }
+      if (sl == 0 && act && cnt != kNbrFallback && ok) {
+        red_add(d.fqx + s, fx);
+        red_add(d.fqy + s, fy);
+        red_add(d.fqz + s, fz);
+        if (PRESS) {
+          red_add(d.pqx + s, px);
+          red_add(d.pqy + s, py);
+          red_add(d.pqz + s, pz);
+        }
+      }
+    }
+    // ---- the particles that need 64-bit sums, one at a time, whole warp
+    uint32_t slow = __ballot_sync(0xffffffffu, sl == 0 && act && (cnt == kNbrFallback || !ok));
+    while (slow) {
+      const int ss = s2 + ((__ffs(slow) - 1) >> 4);
+      slow &= slow - 1;
+      load_row(I, d, ss);
+      I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
+      const uint32_t c2 = d.nbn[ss];
+      if (c2 != kNbrFallback) {  // a term outside the parts' range: the own side again
+        const uint32_t* l2 = d.nbl + (size_t)ss * kNbrCap;
+        const int n2 = (int)c2;
+        for (int k = lane; k < n2; k += 32) {
+          int t, dx, dy, dz;
+          read_entry(l2[k], t, dx, dy, dz);
+          eval_pair<PRESS, FORM, false>(d, R, T, I, t, dx, dy, dz);
+        }
+      } else {  // the list did not fit: walk the cells
+        const int cell = (int)d.scell[ss];
+        if (cell != cached) {  // the segments of the particle's cell (only this path walks cells)
+          int cx, cy, cz;
+          cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+          __syncwarp();
+          build_segments(S, d, R, cx, cy, cz, lane);
+          __syncwarp();
+          cached = cell;
+        }
+        int qn = 0;
+#pragma unroll 1
+        for (int g = 0; g < nseg; g++) {
+          const int tb = S.tb[g], te = S.te[g];
+          if (tb >= te) continue;
+          const int code = S.code[g];
+          int b[2 * REACH];
+#pragma unroll
+          for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+          const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+          const float by = I.pi.y - (float)dy * I.csy, bz = I.pi.z - (float)dz * I.csz;
+          for (int t0 = tb; t0 < te; t0 += 32) {
+            const int t = t0 + lane;
+            bool in = false, own = false;
+            int dx = 0;
+            bool near = false;
+            if (t < te && t != ss) {
+              const float4 pj = __ldg(d.posf + t);
+              dx = fx0 + frame_step<REACH>(t, b);
+              const float ex = (I.pi.x - (float)dx * I.csx) - pj.x, ey = by - pj.y,
+                          ez = bz - pj.z;
+              const float dr2 = ex * ex + ey * ey + ez * ez;
+              in = dr2 < 1.0f;
+              near = fabsf(dr2 - 1.0f) <= kGuard;
+              own = owns(dx, pj.x, I.pi.x, t, ss);
+            }
+            if (__any_sync(0xffffffffu, near) && near) {
+              in = exact_dr2(d, R, d.perm[ss], d.perm[t]) < 1.0;
+            }
+            in = in && own;  // the pairs this particle owns
+            const uint32_t mask = __ballot_sync(0xffffffffu, in);
+            if (in) {
+              const int pos = qn + __popc(mask & lt_mask);
+              QT[pos] = (uint32_t)t;
+              QC[pos] = pack_code(dx, code);
+            }
+            qn += __popc(mask);
+            if (qn >= 32) {
+              __syncwarp();
+              const PairCode pc = unpack_code(QC[lane]);
+              eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+              __syncwarp();
+              if (lane < qn - 32) {
+                QT[lane] = QT[32 + lane];
+                QC[lane] = QC[32 + lane];
+              }
+              __syncwarp();
+              qn -= 32;
+            }
+          }
+        }
+        __syncwarp();
+        if (lane < qn) {
+          const PairCode pc = unpack_code(QC[lane]);
+          eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+        }
+        __syncwarp();
+      }
+      const long long fx = warp_sum_ll(I.fx), fy = warp_sum_ll(I.fy), fz = warp_sum_ll(I.fz);
+      long long px = 0, py = 0, pz = 0;
+      if (PRESS) {
+        px = warp_sum_ll(I.px);
+        py = warp_sum_ll(I.py);
+        pz = warp_sum_ll(I.pz);
+      }
+      if (lane == 0) {
+        red_add(d.fqx + ss, fx);
+        red_add(d.fqy + ss, fy);
+        red_add(d.fqz + ss, fz);
+        if (PRESS) {
+          red_add(d.pqx + ss, px);
+          red_add(d.pqy + ss, py);
+          red_add(d.pqz + ss, pz);
+        }
       }
     }
   }
@@ -1012,8 +1099,12 @@ void launch_force_form(const DevState& d, int nblk, bool with_press, int reach, 
 }
 
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  int form_mask, cudaStream_t st) {
+                  int form_mask, size_t rows, cudaStream_t st) {
   if (nblk == 0) return;
+  if (!fp64) {
+    cudaMemsetAsync(d.fqx, 0, 3 * rows * sizeof(long long), st);
+    if (with_press) cudaMemsetAsync(d.pqx, 0, 3 * rows * sizeof(long long), st);
+  }
   if (fp64) {
     if (with_press)
       k_force_f64<true><<<nblk, kRowBlock, 0, st>>>(d);
@@ -1031,13 +1122,14 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
 
 // ------------------------------------------- precursor conversion
 // idpd_precursor: one warp per 32-row chunk, a particle at a time. A
-// particle of prop_from looks for a particle of prop_near among its pairs
-// within the cutoff: the pass-1 list of the step, or (no list: FP64 arm,
-// list overflow) a sweep of the cells around it with the reference's FP64
-// distance. The draw is Saru(id, time, seed).u32() (saruprng.hpp:239-255,
+// particle of prop_from looks for a particle of prop_near within the cutoff:
+// among its kept list with the cutoff decision of pass 1 (FP32 cell-local
+// distance, FP64 within kGuard of the cutoff), or (no kept list: FP64 arm,
+// no skin, list overflow) in a sweep of the cells around it with the
+// reference's FP64 distance. The draw is Saru(id, time, seed).u32() (saruprng.hpp:239-255,
 // 322-333); properties change in the FP64 rows, so the pair passes see them
 // from the next step's packing on.
-__global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int lists) {
+__global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int kept) {
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   if (!R->prec_on) return;
@@ -1048,11 +1140,23 @@ __global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int lists) 
   for (int s = s0; s < s_end; s++) {
     if (fbits(d.posf[s].w) != from) continue;
     bool near = false;
-    const uint32_t cnt = lists ? (uint32_t)d.nbn[s] : kNbrFallback;
-    if (cnt != kNbrFallback) {
-      const uint32_t* list = d.nbl + (size_t)s * kNbrCap;
-      for (int k = lane; k < (int)cnt; k += 32)
-        near |= fbits(__ldg(d.posf + (list[k] & kRowMask)).w) == near_prop;
+    const uint32_t nv = kept ? (uint32_t)d.vn[s] : kNbrFallback;
+    if (nv != kNbrFallback) {
+      const float4 pi = d.posf[s];
+      const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
+      for (int k = lane; k < (int)nv; k += 32) {
+        int t, dx, dy, dz;
+        read_entry(vl[k], t, dx, dy, dz);
+        const float4 pj = __ldg(d.posf + t);
+        if (fbits(pj.w) != near_prop) continue;
+        const float ex = (pi.x - (float)dx * R->cs_f[0]) - pj.x;
+        const float ey = (pi.y - (float)dy * R->cs_f[1]) - pj.y;
+        const float ez = (pi.z - (float)dz * R->cs_f[2]) - pj.z;
+        const float dr2 = ex * ex + ey * ey + ez * ez;
+        bool in = dr2 < 1.0f;
+        if (fabsf(dr2 - 1.0f) <= kGuard) in = exact_dr2(d, R, d.perm[s], d.perm[t]) < 1.0;
+        near |= in;
+      }
     } else {
       const uint32_t i = d.perm[s];
       int cx, cy, cz;
@@ -1073,8 +1177,8 @@ __global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int lists) 
   }
 }
 
-void launch_precursor(const DevState& d, int nblk, bool lists, cudaStream_t st) {
-  if (nblk > 0) k_precursor<<<nblk, kRowBlock, 0, st>>>(d, lists ? 1 : 0);
+void launch_precursor(const DevState& d, int nblk, bool kept, cudaStream_t st) {
+  if (nblk > 0) k_precursor<<<nblk, kRowBlock, 0, st>>>(d, kept ? 1 : 0);
 }
 
 // -------------------------------------------- neighbour centre of mass

@@ -42,9 +42,9 @@ struct DevState {
   float4 *posf, *velf, *densf;
   float4* poslo;               // low-order parts of the cell-local position
   uint32_t* nbl;               // [N * kNbrCap] in-range neighbours of pass 1 (sorted order)
-  uint16_t* nbn;               // [N] list length, or 0xffff when the list overflowed
-  long long *fqx, *fqy, *fqz;  // pair force, 2^-26 fixed point
-  long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API only)
+  uint16_t* nbn;               // [N] list length (owned pairs), or 0xffff when it overflowed
+  long long *fqx, *fqy, *fqz;  // pair force, 2^-26 fixed point (one block of 3 x capacity)
+  long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API, observation; one block)
   long long *dqx, *dqy, *dqz;  // partial densities in RepDev::dens_unscale units (fine-grained API only)
   double* dens64;              // [3N] partial densities of the plain FP64 arm (sorted order)
   // ---- topology
@@ -156,12 +156,14 @@ struct PairTuning {
 void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
                     cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
-// Precursor conversion after the force pass (lists: the step's pass-1 lists
-// are valid; else the cells are swept).
-void launch_precursor(const DevState& d, int nblk, bool lists, cudaStream_t st);
+// Precursor conversion after the force pass (kept: the kept lists are valid;
+// else the cells are swept).
+void launch_precursor(const DevState& d, int nblk, bool kept, cudaStream_t st);
 void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
+// Pass 2 (rows: the capacity of the force sums, which the FP32 pass zeroes
+// first, since its terms arrive by atomic add).
 void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  int form_mask, cudaStream_t st);
+                  int form_mask, size_t rows, cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
 
 // kernels_chem.cu: one RandomChemEvent (LOCAL_CHEM_EVENT form) on replica 0.
