@@ -342,3 +342,35 @@ def test_replicas_of_different_pair_forms_batched_equal_single():
         a, b = eb.download(k), es.download()
         for key in ("pos", "vel", "acc"):
             assert np.array_equal(a[key], b[key]), (k, key)
+
+
+@pytest.mark.parametrize("reach", [1, 2])
+def test_pair_forces_sum_to_zero_exactly(reach):
+    """Pass 2 evaluates each pair once and gives the other particle the exact
+    negation of the owner's fixed-point term, so the pair forces of a system
+    sum to zero exactly (every force is a whole number of 2^-26 units, summed
+    here as integers), with particles of one cell on both sides
+    of each other, a list overflow and terms past the 32-bit parts among them
+    (a 700-bead cluster)."""
+    box, st, n_amp = mixed_system(seed=22)
+    rng = np.random.default_rng(9)
+    v = rng.normal(size=(700, 3))
+    v *= (0.8 * rng.random(700) ** (1 / 3) / np.linalg.norm(v, axis=1))[:, None]
+    blob = np.mod(st["pos"][0] + v, box)
+    st = dict(st)
+    for k, extra in (("pos", blob), ("vel", rng.normal(size=(700, 3))), ("acc", np.zeros((700, 3))),
+                     ("prop", np.full(700, 2, np.uint32)),
+                     ("amp_id", np.full(700, 0xFFFFFFFF, np.uint32)),
+                     ("unit", np.full(700, 0xFFFFFFFF, np.uint32))):
+        st[k] = np.concatenate([st[k], extra])
+    st["id"] = np.arange(len(st["pos"]), dtype=np.uint32)
+    p = mdpd_params(box, time=7)
+    e = engine_for(p, st)
+    e.set_tuning(reach)
+    e.density()
+    e.force()
+    acc = e.download()["acc"]
+    assert np.any(acc != 0.0)
+    q = acc * 2.0**26
+    assert np.all(np.abs(q) < 2.0**53) and np.all(np.round(q) == q)
+    assert np.array_equal(q.astype(np.int64).sum(axis=0), np.zeros(3, np.int64))

@@ -2,9 +2,9 @@
 precursor bead (here the solvent beads) with a tail bead within the cutoff
 converts to a head when its Saru(id, time, seed) draw is below the
 threshold. Each engine step is compared with the oracle's decisions taken
-from the engine's own state, bit for bit, through the pass-1 lists, the kept
-lists, the FP64 arm (cell sweep) and a particle whose list overflowed (cell
-sweep); a replica without the conversion is left alone."""
+from the engine's own state, bit for bit, through the cell sweep (no kept
+lists), the kept lists, the FP64 arm (cell sweep) and a cluster whose pair
+lists overflow; a replica without the conversion is left alone."""
 import numpy as np
 import pytest
 
@@ -59,7 +59,7 @@ def test_precursor_decisions_match_oracle(flags, skin):
 def test_precursor_through_an_overflowed_list():
     """700 precursors packed within 0.8 of a tail bead: the tail bead and most
     of the precursors have more than 512 pairs within the cutoff, so pass 1
-    keeps no list for them and the conversion sweeps the cells."""
+    keeps no list for them and pass 2 walks their cells."""
     box, st, n_amp = mixed_system(seed=13)
     NB = 700
     rng = np.random.default_rng(5)
