@@ -49,11 +49,12 @@ PAIR_KERNELS = {
               "profile": "force_membrane_1m.md"},
 }
 STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
-KERNELS_PER_STEP = 14          # drift_bin, scan x3, scatter, cell_sort, pack,
-                               # density, force, bonded_kick, cmdrift x3, time
-KERNELS_PER_KEPT_STEP = 17     # drift_disp, rebuild decision, gated bin, gated scan x3,
+KERNELS_PER_STEP = 15          # drift_bin, scan x3, scatter, cell_sort, pack, density,
+                               # density finalize, force, bonded_kick, cmdrift x3, time
+KERNELS_PER_KEPT_STEP = 18     # drift_disp, rebuild decision, gated bin, gated scan x3,
                                # gated scatter / cell_sort / pack, gated list build,
-                               # density, force, bonded_kick, cmdrift x3, time
+                               # density, density finalize, force, bonded_kick, cmdrift x3,
+                               # time
 KERNELS_PER_REORDER = 4        # gather, topology, identity, loc
 
 

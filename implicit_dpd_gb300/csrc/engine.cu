@@ -291,6 +291,7 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   d.fqy = d.fqx + cap;
   d.fqz = d.fqx + 2 * (size_t)cap;
   AL(d.nbl, (size_t)kNbrCap * cap); AL(d.nbn, cap);
+  AL(d.dsum, 4 * (size_t)cap);
   AL(d.topol, 4 * ac);
   AL(d.cf_bend, ac);
   AL(d.reps, h->R);
@@ -308,6 +309,7 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   d.dqx = d.dqy = d.dqz = nullptr;
   CK(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * cc, h->st));
   CK(cudaMemsetAsync(d.err, 0, sizeof(int), h->st));
+  CK(cudaMemsetAsync(d.dsum, 0, sizeof(unsigned long long) * 4 * (size_t)cap, h->st));
   h->cap = cap;
   h->ncell_cap = cc;
   h->nblk_cap = bc;
@@ -354,6 +356,7 @@ int ensure_verlet(idpd_handle* h) {
   if (!d.vl) {
     int rc;
     if ((rc = dalloc(h, &d.vl, (size_t)kVerletCap * h->cap)) || (rc = dalloc(h, &d.vn, h->cap)) ||
+        (rc = dalloc(h, &d.okey, h->cap)) ||
         (rc = dalloc(h, &d.drx, h->cap)) || (rc = dalloc(h, &d.dry, h->cap)) ||
         (rc = dalloc(h, &d.drz, h->cap)) || (rc = dalloc(h, &d.vdev, 1)))
       return rc;
@@ -367,6 +370,15 @@ int ensure_verlet(idpd_handle* h) {
   CK(cudaMemcpyAsync(d.vdev, &v, sizeof(v), cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->vl_dirty = false;
+  invalidate_graph(h);
+  return IDPD_OK;
+}
+
+// The precursor marks of pass 1 (read by the conversion kernel).
+int ensure_phit(idpd_handle* h) {
+  if (!h->prec_any || h->d.phit) return IDPD_OK;
+  int rc = dalloc(h, &h->d.phit, h->cap);
+  if (rc) return rc;
   invalidate_graph(h);
   return IDPD_OK;
 }
@@ -669,11 +681,11 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_scan(d, h->ncell_tot, h->R - 1, h->st);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
-  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
-  launch_force(d, h->nblk, fp64, observe, h->tune, form_mask(h), h->cap, h->st);
+  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->prec_any && d.phit, h->cap, h->st);
+  launch_force(d, h->nblk, fp64, observe, verlet, h->tune, form_mask(h), h->cap, h->st);
   if (h->prec_any) {
     d.prec_count = h->prec_dev;
-    launch_precursor(d, h->nblk, verlet, h->st);
+    launch_precursor(d, h->nblk, !fp64, h->st);
   }
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
@@ -1157,7 +1169,7 @@ int idpd_density(idpd_handle* h) {
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   enqueue_cells(h, false);
-  launch_density(h->d, h->nblk, fp64, h->tune.reach, false, h->st);
+  launch_density(h->d, h->nblk, fp64, h->tune.reach, false, false, h->cap, h->st);
   launch_com(h->d, h->nblk, h->cm64, h->cm_cnt, h->st);
   h->density_valid = true;
   return check_device_error(h);
@@ -1171,7 +1183,7 @@ int idpd_force(idpd_handle* h) {
   if (!h->density_valid) return fail(h, IDPD_ERR_STATE, "idpd_force needs idpd_density on the same positions");
   if ((rc = ensure_aux(h))) return rc;
   const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
-  launch_force(h->d, h->nblk, fp64, true, h->tune, form_mask(h), h->cap, h->st);
+  launch_force(h->d, h->nblk, fp64, true, false, h->tune, form_mask(h), h->cap, h->st);
   launch_fq_to_acc(h->d, h->nblk, h->press64, h->st);
   return check_device_error(h);
 }
@@ -1229,7 +1241,7 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
   if (h->chem_on && h->chem_stopped)
     return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num: the run has ended");
-  if ((rc = ensure_verlet_ready(h))) return rc;
+  if ((rc = ensure_verlet_ready(h)) || (rc = ensure_phit(h))) return rc;
   std::vector<uint32_t> time;  // step counters, to pick the steps that observe
   if (h->obs_period > 0) {
     if ((rc = ensure_obs(h))) return rc;
@@ -1368,9 +1380,9 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[3], h->st));
   if (verlet) launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
-  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->st);
+  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, false, h->cap, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_force(d, h->nblk, fp64, false, h->tune, form_mask(h), h->cap, h->st);
+  launch_force(d, h->nblk, fp64, false, verlet, h->tune, form_mask(h), h->cap, h->st);
   CK(cudaEventRecord(ev[6], h->st));
   launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[7], h->st));

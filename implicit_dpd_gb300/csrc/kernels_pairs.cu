@@ -133,19 +133,20 @@ __device__ __forceinline__ PairCode unpack_code(uint32_t c) {
 // Neighbour list entry (32 bits): the candidate's sorted row (25 bits) and
 // its frame cell's offset from the particle's frame cell, dx, dy, dz + 1 in
 // 2 bits each. kNbrFallback marks a particle whose list did not fit (the
-// next pass walks its cells again). A pass-1 list holds the pairs within the
-// cutoff that the particle owns (owns()).
+// next pass walks its cells again). Kept lists hold the candidates and
+// pass-1 lists the pairs within the cutoff that the particle owns (owns()).
 constexpr uint32_t kNbrFallback = 0xffffu;
 constexpr int kRowBits = 25;
 constexpr uint32_t kRowMask = (1u << kRowBits) - 1u;
 
-// Pass 2 evaluates each pair once, from the side of the particle that owns
-// it: the frame offset dx of the other particle decides when nonzero, else
-// (the same frame cell column) the larger cell-local x of the step, else the
-// larger sorted row. Every path of a step decides on the same FP32 rows, so
-// the two particles of a pair always agree, and each particle owns about
-// half of its pairs (those on the +x side of the plane through it), which
-// keeps the two particles of a half-warp pair in pass 2 near equal work.
+// Both pair passes take each pair once, from the side of the particle that
+// owns it: the frame offset dx of the other particle decides when nonzero,
+// else (the same frame cell column) the larger cell-local x, else the larger
+// sorted row. The x is that of the step (no kept lists) or of the kept
+// lists' build (okey): rows and frame cells do not change between builds, so
+// the two particles of a pair always agree. Each particle owns about half of
+// its pairs (those on the +x side of the plane through it), which keeps the
+// two particles of a half-warp pair in pass 2 near equal work.
 __device__ __forceinline__ bool owns(int dx, float xj, float xi, int t, int s) {
   if (dx != 0) return dx > 0;
   return xj != xi ? xj > xi : t > s;
@@ -179,15 +180,19 @@ __device__ __forceinline__ void add_weight(uint32_t& q0, uint32_t& q1, uint32_t&
   q2 += pr == 2 ? v : 0u;
 }
 
-// One warp per particle. Without kept lists: phase A sweeps the neighbour
-// segments 32 candidates at a time and appends the pairs within the cutoff
-// 1 to a list in shared memory; phase B takes the density weights from that
-// list with every lane busy and copies the list out for pass 2 (a particle
-// whose list overflows takes its weights during a second sweep). With kept
-// lists (VERLET): one pass over the particle's kept list tests each
-// candidate, adds its weight and appends it to the list of pass 2 when the
-// particle owns the pair.
-template <int REACH, bool VERLET>
+// One warp per particle, over the pairs it owns (owns(); the other particle
+// gets the same weight by atomic add). Without kept lists: phase A sweeps the
+// neighbour segments 32 candidates at a time and appends the owned pairs
+// within the cutoff 1 to a list in shared memory; phase B takes the density
+// weights from that list with every lane busy and copies the list out for
+// pass 2 (a particle whose list overflows takes its weights during a second
+// sweep). With kept lists (VERLET, owned candidates only): one pass over the
+// particle's kept list tests each candidate, adds its weight and appends it
+// to the list of pass 2. Each particle's own total is added to its sums in
+// dsum as well; k_dens_finalize turns them into the FP32 densities.
+// With MARKS, the precursor conversion's marks (phit): a pair of prop_from
+// and prop_near within the cutoff marks the prop_from particle.
+template <int REACH, bool VERLET, bool MARKS>
 __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t lst[kWarps][kNbrCap];
@@ -203,19 +208,21 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
   const double cutd2d = (double)R->wrd * (double)R->wrd;
   const float inv_rd = R->winv_rd, wnorm = R->wnorm, pre = R->dens_prescale;
   const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
+  const bool prec = MARKS && R->prec_on;
   constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
   for (int s = s0; s < s_end; s++) {
     const float4 pi = d.posf[s];
-    const uint32_t si = d.perm[s];
-    int nl = 0, nu = 0;  // pairs within the cutoff, owned ones among them
-    int nw = 0;          // bound on the weighted pairs
-    bool swept = true;   // the pairs came from a sweep of the cells (list out below)
+    const uint32_t si = d.perm[s], pri = fbits(pi.w);
+    const float ki = VERLET ? d.okey[s] : pi.x;  // the ownership key of the step
+    int nl = 0;  // owned pairs within the cutoff
+    int nw = 0;  // bound on the weighted pairs
+    bool hit = false;
     uint32_t q0 = 0, q1 = 0, q2 = 0;
-    // weight of one candidate; called by every lane together (valid = false
-    // for lanes without one) so that the rare FP64 recheck is warp-uniform.
-    // Returns whether the pair lies within the cutoff 1.
+    // weight of one owned candidate, to both particles; called by every lane
+    // together (valid = false for lanes without one) so that the rare FP64
+    // recheck is warp-uniform. Returns whether the pair lies within the cutoff 1.
     auto test = [&](bool valid, int t, int dx, int dy, int dz, float4 pj, bool list_known) {
       const float ex = (pi.x - (float)dx * csx) - pj.x;
       const float ey = (pi.y - (float)dy * csy) - pj.y;
@@ -235,11 +242,21 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
           ind = in1 && (near2 ? (e2 < cutd2d && e2 != 0.0) : (dr2 < cutd2 && dr2 >= 1.0e-10f));
         }
       }
-      if (ind) add_weight(q0, q1, q2, fbits(pj.w), dens_weight(dr2, warren, inv_rd, wnorm, pre));
+      const uint32_t prj = fbits(pj.w);
+      if (ind) {
+        const uint32_t w = dens_weight(dr2, warren, inv_rd, wnorm, pre);
+        add_weight(q0, q1, q2, prj, w);
+        atomicAdd(d.dsum + 4 * (size_t)t + (pri & 3u), (unsigned long long)w);
+      }
+      if (MARKS && prec && in1) {
+        hit |= pri == R->prec_from && prj == R->prec_near;
+        if (prj == R->prec_from && pri == R->prec_near) d.phit[t] = 1;
+      }
       return in1;
     };
     const uint32_t nv = VERLET ? (uint32_t)d.vn[s] : kNbrFallback;
     bool fits = true;
+    bool swept = true;  // the pairs came from a sweep of the cells (list out below)
     if (VERLET && nv != kNbrFallback) {
       // ---- the particle's kept list: test, weight and list out in one pass
       swept = false;
@@ -254,18 +271,16 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
         int t, dx, dy, dz;
         read_entry(e, t, dx, dy, dz);
         if (!valid) t = s;
-        const float4 pj = __ldg(d.posf + t);
-        const bool in1 = test(valid, t, dx, dy, dz, pj, false);
-        const bool put = in1 && owns(dx, pj.x, pi.x, t, s);
-        const uint32_t mo = __ballot_sync(0xffffffffu, put);
-        if (put) {
-          const int pos = nu + __popc(mo & lt_mask);
+        const bool in1 = test(valid, t, dx, dy, dz, __ldg(d.posf + t), false);
+        const uint32_t mask = __ballot_sync(0xffffffffu, in1);
+        if (in1) {
+          const int pos = nl + __popc(mask & lt_mask);
           if (pos < kNbrCap) out[pos] = e;
         }
-        nu += __popc(mo);
+        nl += __popc(mask);
       }
       nw = (int)nv;
-      fits = nu <= kNbrCap;
+      fits = nl <= kNbrCap;
     } else {
       const int cell = (int)d.scell[s];
       if (cell != cached) {
@@ -276,7 +291,7 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
         __syncwarp();
         cached = cell;
       }
-      // ---- phase A: the pairs within the cutoff 1
+      // ---- phase A: the owned pairs within the cutoff 1
 #pragma unroll 1
       for (int g = 0; g < nseg; g++) {
         const int tb = S.tb[g], te = S.te[g];
@@ -294,11 +309,13 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
           if (t < te && t != s) {
             const float4 pj = __ldg(d.posf + t);
             ddx = frame_step<REACH>(t, b);
-            const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
-                        ez = bz - pj.z;
-            const float dr2 = ex * ex + ey * ey + ez * ez;
-            in1 = dr2 < 1.0f;
-            near = fabsf(dr2 - 1.0f) <= kGuard;
+            if (owns(fx0 + ddx, VERLET ? d.okey[t] : pj.x, ki, t, s)) {
+              const float ex = (pi.x - (float)(fx0 + ddx) * csx) - pj.x, ey = by - pj.y,
+                          ez = bz - pj.z;
+              const float dr2 = ex * ex + ey * ey + ez * ez;
+              in1 = dr2 < 1.0f;
+              near = fabsf(dr2 - 1.0f) <= kGuard;
+            }
           }
           if (__any_sync(0xffffffffu, near)) {
             if (near) in1 = exact_dr2(d, R, si, d.perm[t]) < 1.0;
@@ -337,30 +354,19 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
           const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
           for (int t0 = tb; t0 < te; t0 += 32) {
             const int t = t0 + lane;
-            const bool valid = t < te && t != s;
-            test(valid, valid ? t : s, fx0 + frame_step<REACH>(t, b), dy, dz,
-                 valid ? __ldg(d.posf + t) : pi, false);
+            const int dx = fx0 + frame_step<REACH>(t, b);
+            const float4 pj = t < te ? __ldg(d.posf + t) : pi;
+            const bool valid =
+                t < te && t != s && owns(dx, VERLET ? d.okey[t] : pj.x, ki, t, s);
+            test(valid, valid ? t : s, dx, dy, dz, pj, false);
           }
         }
       }
     }
     __syncwarp();
-    if (swept && fits) {  // list out for pass 2: the owned pairs, coalesced
+    if (swept && fits) {  // list out for pass 2, coalesced
       uint32_t* out = d.nbl + (size_t)s * kNbrCap;
-      for (int k0 = 0; k0 < nl; k0 += 32) {
-        const int k = k0 + lane;
-        uint32_t e = 0u;
-        bool own = false;
-        if (k < nl) {
-          e = L[k];
-          int t, dx, dy, dz;
-          read_entry(e, t, dx, dy, dz);
-          own = owns(dx, __ldg(&d.posf[t].x), pi.x, t, s);
-        }
-        const uint32_t mo = __ballot_sync(0xffffffffu, own);
-        if (own) out[nu + __popc(mo & lt_mask)] = e;
-        nu += __popc(mo);
-      }
+      for (int k = lane; k < nl; k += 32) out[k] = L[k];
     }
     // each weight is below 2^23, so up to 512 weighted pairs total below
     // 2^32 (nw bounds them: the kept list's length, or the pairs in range)
@@ -378,19 +384,36 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
         a2 += __shfl_xor_sync(0xffffffffu, a2, o);
       }
     }
+    if (MARKS) hit = __any_sync(0xffffffffu, hit);
     if (lane == 0) {
-      const float u = R->dens_unscale_f;
-      d.densf[s] = make_float4(fix_to_float((long long)a0, u), fix_to_float((long long)a1, u),
-                               fix_to_float((long long)a2, u), 0.0f);
-      d.nbn[s] = fits ? (uint16_t)nu : (uint16_t)kNbrFallback;
-      if (d.dqx) {
-        d.dqx[s] = (long long)a0;
-        d.dqy[s] = (long long)a1;
-        d.dqz[s] = (long long)a2;
-      }
+      unsigned long long* q = d.dsum + 4 * (size_t)s;
+      if (a0) atomicAdd(q, a0);
+      if (a1) atomicAdd(q + 1, a1);
+      if (a2) atomicAdd(q + 2, a2);
+      d.nbn[s] = fits ? (uint16_t)nl : (uint16_t)kNbrFallback;
+      if (MARKS && hit) d.phit[s] = 1;
     }
     __syncwarp();
   }
+}
+
+// The FP32 densities of pass 1 from its fixed-point sums (and the fixed-point
+// densities of the fine-grained API); the sums are zeroed for the next pass.
+__global__ void __launch_bounds__(kRowBlock) k_dens_finalize(DevState d) {
+  const int r = d.blk_rep[blockIdx.x];
+  const int s = d.blk_row[blockIdx.x] + threadIdx.x;
+  const RepDev* R = d.reps + r;
+  if (s >= R->row_off + R->n) return;
+  unsigned long long* q = d.dsum + 4 * (size_t)s;
+  const long long a0 = (long long)q[0], a1 = (long long)q[1], a2 = (long long)q[2];
+  const float u = R->dens_unscale_f;
+  d.densf[s] = make_float4(fix_to_float(a0, u), fix_to_float(a1, u), fix_to_float(a2, u), 0.0f);
+  if (d.dqx) {
+    d.dqx[s] = a0;
+    d.dqy[s] = a1;
+    d.dqz[s] = a2;
+  }
+  q[0] = q[1] = q[2] = 0ull;
 }
 
 // The kept lists (rebuild steps only). The particles of one cell share its
@@ -401,9 +424,11 @@ __global__ void __launch_bounds__(kRowBlock, 10) k_density_f32(DevState d) {
 // is in range append it to that particle's list in one coalesced store. A
 // candidate is kept when closer than 1 + skin in FP32 (with a margin: the
 // list only has to hold every pair that can come within the cutoff before
-// the next rebuild). The warp of a 32-row chunk takes the cells whose first
-// row lies in the chunk. Also records each row's delta_sumr for the
-// displacement test.
+// the next rebuild). Only the candidates the particle owns are kept (owns()
+// on the cell-local x of the build, kept in okey): the stencil's -x third is
+// never queued. The warp of a 32-row chunk takes the cells whose first row
+// lies in the chunk. Also records each row's delta_sumr for the displacement
+// test.
 template <int REACH>
 __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   __shared__ SegTable seg[kWarps];
@@ -462,11 +487,15 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
       // the lanes whose candidate is in range of particle k write it to k's
       // list, consecutive lanes to consecutive slots
       auto round = [&](float qx, float qy, float qz, uint32_t e, int t) {
+        const bool fwd = ((e >> kRowBits) & 3u) == 2u;  // frame offset +1: owned by all
 #pragma unroll 4
         for (int k = 0; k < nb; k++) {
           const float4 pk = P[k];
           const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
-          const bool in = ex * ex + ey * ey + ez * ez < rv2 && t != b0 + k;
+          // owns(): qx is the candidate's cell-local x when its offset is 0
+          // (a particle never owns itself)
+          const bool in = ex * ex + ey * ey + ez * ez < rv2 &&
+                          (fwd || qx > pk.x || (qx == pk.x && t > b0 + k));
           const uint32_t m = __ballot_sync(0xffffffffu, in);
           const int base = __shfl_sync(0xffffffffu, cnt, k);
           const int pos = base + __popc(m & lt_mask);
@@ -499,7 +528,7 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
             const float ox = fmaxf(fmaxf(lox - qx, qx - hix), 0.0f);
             const float oy = fmaxf(fmaxf(loy - qy, qy - hiy), 0.0f);
             const float oz = fmaxf(fmaxf(loz - qz, qz - hiz), 0.0f);
-            keep = ox * ox + oy * oy + oz * oz < rv2;
+            keep = fx >= 0 && ox * ox + oy * oy + oz * oz < rv2;
           }
           const uint32_t mask = __ballot_sync(0xffffffffu, keep);
           if (keep) {
@@ -536,6 +565,7 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
       __syncwarp();
       if (lane < nb) {
         d.vn[me] = cnt <= kVerletCap ? (uint16_t)cnt : (uint16_t)kNbrFallback;
+        d.okey[me] = pm.x;
         const uint32_t i = d.perm[me];
         d.drx[me] = d.dsx[i];
         d.dry[me] = d.dsy[i];
@@ -622,19 +652,32 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   }
 }
 
-void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
-                    cudaStream_t st) {
-  if (nblk == 0) return;
-  if (fp64)
-    k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
-  else if (verlet && reach == 2)
-    k_density_f32<2, true><<<nblk, kRowBlock, 0, st>>>(d);
+template <bool MARKS>
+void launch_density_f32(const DevState& d, int nblk, int reach, bool verlet, cudaStream_t st) {
+  if (verlet && reach == 2)
+    k_density_f32<2, true, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
   else if (verlet)
-    k_density_f32<1, true><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<1, true, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
   else if (reach == 2)
-    k_density_f32<2, false><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<2, false, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
   else
-    k_density_f32<1, false><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<1, false, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
+}
+
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet, bool marks,
+                    size_t rows, cudaStream_t st) {
+  if (nblk == 0) return;
+  if (fp64) {
+    k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
+    return;
+  }
+  if (marks) {
+    cudaMemsetAsync(d.phit, 0, rows, st);
+    launch_density_f32<true>(d, nblk, reach, verlet, st);
+  } else {
+    launch_density_f32<false>(d, nblk, reach, verlet, st);
+  }
+  k_dens_finalize<<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 // ------------------------------------------------------------- pass 2
@@ -837,7 +880,7 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
 // only). One launch per pair form present: a block whose replica has another
 // form returns at once.
 template <int REACH, bool PRESS, int FORM>
-__global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
+__global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d, int kept) {
   __shared__ SegTable seg[kWarps];
   __shared__ uint32_t qt[kWarps][64], qc[kWarps][64];
   __shared__ PairTables T;
@@ -950,7 +993,7 @@ __global__ void __launch_bounds__(kRowBlock, 8) k_force_f32(DevState d) {
               const float dr2 = ex * ex + ey * ey + ez * ez;
               in = dr2 < 1.0f;
               near = fabsf(dr2 - 1.0f) <= kGuard;
-              own = owns(dx, pj.x, I.pi.x, t, ss);
+              own = owns(dx, kept ? d.okey[t] : pj.x, kept ? d.okey[ss] : I.pi.x, t, ss);
             }
             if (__any_sync(0xffffffffu, near) && near) {
               in = exact_dr2(d, R, d.perm[ss], d.perm[t]) < 1.0;
@@ -1084,22 +1127,23 @@ __global__ void __launch_bounds__(kRowBlock) k_force_f64(DevState d) {
 }
 
 template <int FORM>
-void launch_force_form(const DevState& d, int nblk, bool with_press, int reach, cudaStream_t st) {
+void launch_force_form(const DevState& d, int nblk, bool with_press, int reach, int kept,
+                       cudaStream_t st) {
   if (reach == 2) {
     if (with_press)
-      k_force_f32<2, true, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+      k_force_f32<2, true, FORM><<<nblk, kRowBlock, 0, st>>>(d, kept);
     else
-      k_force_f32<2, false, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+      k_force_f32<2, false, FORM><<<nblk, kRowBlock, 0, st>>>(d, kept);
   } else {
     if (with_press)
-      k_force_f32<1, true, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+      k_force_f32<1, true, FORM><<<nblk, kRowBlock, 0, st>>>(d, kept);
     else
-      k_force_f32<1, false, FORM><<<nblk, kRowBlock, 0, st>>>(d);
+      k_force_f32<1, false, FORM><<<nblk, kRowBlock, 0, st>>>(d, kept);
   }
 }
 
-void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  int form_mask, size_t rows, cudaStream_t st) {
+void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, bool kept,
+                  const PairTuning& tu, int form_mask, size_t rows, cudaStream_t st) {
   if (nblk == 0) return;
   if (!fp64) {
     cudaMemsetAsync(d.fqx, 0, 3 * rows * sizeof(long long), st);
@@ -1113,23 +1157,21 @@ void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const
     return;
   }
   if (form_mask & (1 << IDPD_FORM_MDPD_K))
-    launch_force_form<IDPD_FORM_MDPD_K>(d, nblk, with_press, tu.reach, st);
+    launch_force_form<IDPD_FORM_MDPD_K>(d, nblk, with_press, tu.reach, kept ? 1 : 0, st);
   if (form_mask & (1 << IDPD_FORM_PAIRWISE_K))
-    launch_force_form<IDPD_FORM_PAIRWISE_K>(d, nblk, with_press, tu.reach, st);
+    launch_force_form<IDPD_FORM_PAIRWISE_K>(d, nblk, with_press, tu.reach, kept ? 1 : 0, st);
   if (form_mask & (1 << IDPD_FORM_WARREN_K))
-    launch_force_form<IDPD_FORM_WARREN_K>(d, nblk, with_press, tu.reach, st);
+    launch_force_form<IDPD_FORM_WARREN_K>(d, nblk, with_press, tu.reach, kept ? 1 : 0, st);
 }
 
 // ------------------------------------------- precursor conversion
 // idpd_precursor: one warp per 32-row chunk, a particle at a time. A
 // particle of prop_from looks for a particle of prop_near within the cutoff:
-// among its kept list with the cutoff decision of pass 1 (FP32 cell-local
-// distance, FP64 within kGuard of the cutoff), or (no kept list: FP64 arm,
-// no skin, list overflow) in a sweep of the cells around it with the
-// reference's FP64 distance. The draw is Saru(id, time, seed).u32() (saruprng.hpp:239-255,
+// the mark pass 1 left when it took such a pair (phit), or (FP64 arm) a sweep
+// of the cells around it with the reference's FP64 distance. The draw is Saru(id, time, seed).u32() (saruprng.hpp:239-255,
 // 322-333); properties change in the FP64 rows, so the pair passes see them
 // from the next step's packing on.
-__global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int kept) {
+__global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int marks) {
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   if (!R->prec_on) return;
@@ -1140,23 +1182,8 @@ __global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int kept) {
   for (int s = s0; s < s_end; s++) {
     if (fbits(d.posf[s].w) != from) continue;
     bool near = false;
-    const uint32_t nv = kept ? (uint32_t)d.vn[s] : kNbrFallback;
-    if (nv != kNbrFallback) {
-      const float4 pi = d.posf[s];
-      const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
-      for (int k = lane; k < (int)nv; k += 32) {
-        int t, dx, dy, dz;
-        read_entry(vl[k], t, dx, dy, dz);
-        const float4 pj = __ldg(d.posf + t);
-        if (fbits(pj.w) != near_prop) continue;
-        const float ex = (pi.x - (float)dx * R->cs_f[0]) - pj.x;
-        const float ey = (pi.y - (float)dy * R->cs_f[1]) - pj.y;
-        const float ez = (pi.z - (float)dz * R->cs_f[2]) - pj.z;
-        const float dr2 = ex * ex + ey * ey + ez * ez;
-        bool in = dr2 < 1.0f;
-        if (fabsf(dr2 - 1.0f) <= kGuard) in = exact_dr2(d, R, d.perm[s], d.perm[t]) < 1.0;
-        near |= in;
-      }
+    if (marks) {
+      near = d.phit[s] != 0;
     } else {
       const uint32_t i = d.perm[s];
       int cx, cy, cz;
@@ -1177,8 +1204,8 @@ __global__ void __launch_bounds__(kRowBlock) k_precursor(DevState d, int kept) {
   }
 }
 
-void launch_precursor(const DevState& d, int nblk, bool kept, cudaStream_t st) {
-  if (nblk > 0) k_precursor<<<nblk, kRowBlock, 0, st>>>(d, kept ? 1 : 0);
+void launch_precursor(const DevState& d, int nblk, bool marks, cudaStream_t st) {
+  if (nblk > 0) k_precursor<<<nblk, kRowBlock, 0, st>>>(d, marks ? 1 : 0);
 }
 
 // -------------------------------------------- neighbour centre of mass

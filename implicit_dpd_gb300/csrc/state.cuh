@@ -47,6 +47,7 @@ struct DevState {
   long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API, observation; one block)
   long long *dqx, *dqy, *dqz;  // partial densities in RepDev::dens_unscale units (fine-grained API only)
   double* dens64;              // [3N] partial densities of the plain FP64 arm (sorted order)
+  unsigned long long* dsum;    // [4N] pass-1 partial densities by property, fixed point (zero between passes)
   // ---- topology
   uint32_t* topol;  // [4 * total molecules] storage rows
   float* cf_bend;   // [total molecules]
@@ -61,9 +62,11 @@ struct DevState {
   double* rep_mean;  // [R * 3]
   int* err;          // device error word (0 = ok)
   unsigned long long* prec_count;  // [R] precursor conversions per replica
+  uint8_t* phit;                   // [N] pass 1 took a pair of the conversion's properties
   // ---- neighbour lists kept between rebuilds (null when the skin is 0)
   uint32_t* vl;                // [N * kVerletCap] pairs within 1 + skin at the last rebuild
   uint16_t* vn;                // [N] list length, or 0xffff when it did not fit
+  float* okey;                 // [N] cell-local x at the last build (pair ownership)
   double *drx, *dry, *drz;     // delta_sumr at the last rebuild (sorted order)
   struct VerletDev* vdev;
 };
@@ -153,17 +156,20 @@ struct PairTuning {
   int reach;       // 1: cells of the cutoff, 27-cell stencil; 2: half cells, 125-cell stencil
   float skin;      // > 0: lists of pairs within 1 + skin kept until a rebuild (reach 1)
 };
-void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet,
-                    cudaStream_t st);
+// Pass 1 and its densities (verlet: over the kept lists; marks: also the
+// precursor marks, zeroed first over rows, the buffer's capacity).
+void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet, bool marks,
+                    size_t rows, cudaStream_t st);
+// Precursor conversion after the force pass (marks: the FP32 pass 1 left its
+// marks; else the cells are swept).
+void launch_precursor(const DevState& d, int nblk, bool marks, cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
-// Precursor conversion after the force pass (kept: the kept lists are valid;
-// else the cells are swept).
-void launch_precursor(const DevState& d, int nblk, bool kept, cudaStream_t st);
 void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
-// Pass 2 (rows: the capacity of the force sums, which the FP32 pass zeroes
-// first, since its terms arrive by atomic add).
-void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, const PairTuning& tu,
-                  int form_mask, size_t rows, cudaStream_t st);
+// Pass 2 (kept: pass 1 ran over the kept lists; rows: the capacity of the
+// force sums, which the FP32 pass zeroes first, since its terms arrive by
+// atomic add).
+void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, bool kept,
+                  const PairTuning& tu, int form_mask, size_t rows, cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
 
 // kernels_chem.cu: one RandomChemEvent (LOCAL_CHEM_EVENT form) on replica 0.
