@@ -493,9 +493,9 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
           const float4 pk = P[k];
           const float ex = pk.x - qx, ey = pk.y - qy, ez = pk.z - qz;
           // owns(): qx is the candidate's cell-local x when its offset is 0
-          // (a particle never owns itself)
-          const bool in = ex * ex + ey * ey + ez * ez < rv2 &&
-                          (fwd || qx > pk.x || (qx == pk.x && t > b0 + k));
+          // (a particle never owns itself); predicate logic, no branches
+          const bool own = fwd | (qx > pk.x) | ((qx == pk.x) & (t > b0 + k));
+          const bool in = (ex * ex + ey * ey + ez * ez < rv2) & own;
           const uint32_t m = __ballot_sync(0xffffffffu, in);
           const int base = __shfl_sync(0xffffffffu, cnt, k);
           const int pos = base + __popc(m & lt_mask);
