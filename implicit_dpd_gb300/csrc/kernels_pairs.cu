@@ -2,16 +2,18 @@
 //   pass 1, CalcDensity::operator() (nbdf_calculator.hpp:11-60);
 //   pass 2, CalcForceEpEpDPD::operator() (nbdf_calculator.hpp:63-145).
 //
-// FP32 passes (the engine): one warp per particle. The warp caches the
-// neighbour-cell segments of the particle's cell in shared memory, sweeps
-// each segment 32 candidates at a time (coalesced float4 loads), and for
-// pass 2 appends the in-range pairs to a warp queue that is evaluated 32
-// pairs at a time with every lane busy. Pair vectors come from cell-local
-// FP32 coordinates; cutoff decisions within kGuard of the cutoff are re-taken
-// in FP64 from the FP64 positions as the reference takes them; pairs within
-// 0.01 of the cutoff take 1 - r from the compensated (hi + lo) coordinates;
-// every pair term is summed as a 64-bit fixed-point integer, so the result is
-// independent of the visiting order, of the cell size and of the launch shape.
+// FP32 passes (the engine): each pair is taken once, by the particle that
+// owns it (owns()), and its term goes to both particles. Pass 1 runs one warp
+// per particle over its kept list or its cells (the neighbour-cell segments
+// cached in shared memory, swept 32 candidates at a time with coalesced
+// float4 loads) and writes the owned pairs within the cutoff as the list of
+// pass 2, which runs two particles per warp, 16 lanes each. Pair vectors come
+// from cell-local FP32 coordinates; cutoff decisions within kGuard of the
+// cutoff are re-taken in FP64 from the FP64 positions as the reference takes
+// them; pairs within 0.01 of the cutoff take 1 - r from the compensated
+// (hi + lo) coordinates; every pair term is summed as a 64-bit fixed-point
+// integer, so the result is independent of the visiting order, of the cell
+// size and of the launch shape.
 //
 // FP64 passes (the plain single-system baseline): one thread per particle,
 // FP64 throughout, FP64 sums in cell order.
@@ -872,7 +874,7 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
 // its term goes to both particles (Newton's third law in exact fixed point: the
 // sums equal those of the reference's two evaluations up to the FP32
 // rounding of one of them). A warp takes two particles at a time, 16 lanes
-// each, over the owned pairs at the front of their pass-1 lists; the sums
+// each, over their pass-1 lists (owned pairs only); the sums
 // start at zero (launch_force) and every term arrives by atomic add. A
 // particle whose list overflowed walks its cells again with the whole warp
 // and queues the in-range pairs in shared memory; a particle with a term

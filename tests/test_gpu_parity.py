@@ -288,10 +288,8 @@ def test_cell_reach_gives_bit_identical_trajectories():
 def test_dense_membrane_density_force_match_oracle(rho):
     """The compacted membrane regime (~150 neighbours per bead at rho 30)
     fills several 32-pair rounds per particle; rho 90 (~380 pairs within the
-    cutoff) fills long lists; at rho 160 (~670 pairs, > 512) the pass-1 lists
-    overflow and pass 2 walks the cells again, and with a skin of 0.2 the
-    kept lists (~1,160 candidates, > 1,024) overflow too and pass 1 sweeps the
-    cells. Fine-grained passes, then one graph step with kept lists."""
+    cutoff, ~190 owned) and rho 160 (~670, ~335 owned) fill long lists.
+    Fine-grained passes, then one graph step with kept lists."""
     box = np.array([7.0, 7.0, 5.0]) if rho < 50 else np.array([5.0, 5.0, 5.0])
     rng = np.random.default_rng(12)
     st = configs.liquid(box, rho, seed=12, prop=1)
@@ -374,3 +372,42 @@ def test_pair_forces_sum_to_zero_exactly(reach):
     q = acc * 2.0**26
     assert np.all(np.abs(q) < 2.0**53) and np.all(np.round(q) == q)
     assert np.array_equal(q.astype(np.int64).sum(axis=0), np.zeros(3, np.int64))
+
+
+def test_list_overflows_match_oracle():
+    """rho 400 (~1,680 pairs within the cutoff, ~840 owned): every pass-1
+    list overflows its 512 slots, so pass 1 weighs its pairs in a second
+    sweep and pass 2 walks the cells again; with a skin of 0.2 the kept lists
+    (~1,450 owned candidates, > 1,024) overflow too and pass 1 sweeps the
+    cells with the build's ownership. Densities, forces and one kept-list
+    step against the oracle; the pair forces sum to zero exactly."""
+    box = np.array([3.7, 3.7, 3.7])
+    rng = np.random.default_rng(40)
+    st = configs.liquid(box, 400.0, seed=40, prop=1)
+    st["prop"] = rng.integers(0, 3, len(st["pos"])).astype(np.uint32)
+    p = mdpd_params(box, time=5)
+    dens, cm, cnt, acc, press = oracle_forces(p, st)
+    for reach in (1, 2):
+        e = engine_for(p, st)
+        e.set_tuning(reach)
+        e.density()
+        d = e.download_aux(density=True)
+        assert np.abs(d["dens"] - dens).max() / np.abs(dens).max() < FORCE_TOL
+        e.force()
+        got = e.download()["acc"]
+        worst, agg = rel_force_err(got, acc)
+        assert worst < FORCE_TOL, (reach, worst, agg)
+        q = got * 2.0**26
+        assert np.all(np.abs(q) < 2.0**53) and np.all(np.round(q) == q)
+        assert np.array_equal(q.astype(np.int64).sum(axis=0), np.zeros(3, np.int64))
+    e = engine_for(p, st)
+    e.set_tuning(1, 0.2)
+    s0 = e.download()
+    e.step(1)
+    s1 = e.download()
+    po = type(p).from_buffer_copy(p)
+    ref = {k: s0[k].copy() for k in ("pos", "vel", "acc", "id", "prop")}
+    O.md_step(po, ref, nthreads=os.cpu_count() or 4)
+    assert np.array_equal(s1["pos"], ref["pos"])
+    worst, agg = rel_force_err(s1["acc"], ref["acc"])
+    assert worst < FORCE_TOL, ("kept lists", worst, agg)
