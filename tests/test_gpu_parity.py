@@ -381,7 +381,7 @@ def test_list_overflows_match_oracle():
     (~1,450 owned candidates, > 1,024) overflow too and pass 1 sweeps the
     cells with the build's ownership. Densities, forces and one kept-list
     step against the oracle; the pair forces sum to zero exactly."""
-    box = np.array([3.7, 3.7, 3.7])
+    box = np.array([5.0, 5.0, 5.0])  # the fine-grained density pass wants >= 5 cells per axis
     rng = np.random.default_rng(40)
     st = configs.liquid(box, 400.0, seed=40, prop=1)
     st["prop"] = rng.integers(0, 3, len(st["pos"])).astype(np.uint32)
