@@ -111,3 +111,21 @@ def test_invalid_arguments_are_rejected(lib):
     bad = IdpdConfig(n_replicas=0)
     assert lib.idpd_create(C.byref(bad), C.byref(h)) == 1
     assert lib.idpd_create(None, C.byref(h)) == 1
+
+
+def test_cpp_adapters_compile_and_link(lib, tmp_path):
+    """The C++ adapters (include/idpd/reference_api.hpp) compile against the
+    reference's names (the FDPS stand-in of the oracle) as the adapter test's
+    host program uses them, and link against the library; no GPU needed."""
+    from implicit_dpd_gb300.engine import LIB_PATH
+    exe = os.path.join(str(tmp_path), "reference_api_run")
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(B.nvcc())), "lib64")
+    libdir = os.path.dirname(LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(ROOT, "oracle", "ps_standin"),
+           os.path.join(ROOT, "tests", "cpp", "reference_api_run.cpp"), "-o", exe,
+           "-L", libdir, "-lidpd_engine", "-Wl,-rpath," + libdir,
+           "-L", cuda_lib, "-Wl,-rpath," + cuda_lib, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert os.path.exists(exe)
