@@ -49,6 +49,11 @@ PAIR_KERNELS = {
               "profile": "force_membrane_1m.md"},
 }
 STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
+# Algorithmic lane operations per in-range ordered pair (the reference
+# evaluates every pair from both sides): the force pass ~54 FP32 + ~75 INT32
+# (the Saru hash and draws) + 5 SFU (sqrt r, rcp, sqrt w, log, cos); the
+# density pass ~12 FP32 + 1 SFU.
+OPS_PER_ORDERED_PAIR = {"force": 134, "density": 13}
 KERNELS_PER_STEP = 15          # drift_bin, scan x3, scatter, cell_sort, pack, density,
                                # density finalize, force, bonded_kick, cmdrift x3, time
 KERNELS_PER_KEPT_STEP = 18     # drift_disp, rebuild decision, gated bin, gated scan x3,
@@ -118,6 +123,14 @@ class Dist:
         self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
         return float(t.item())
 
+    def gather(self, obj):
+        """Every rank's obj, in rank order (host objects over gloo)."""
+        if not self.pg:
+            return [obj]
+        out = [None] * self.td.get_world_size()
+        self.td.all_gather_object(out, obj)
+        return out
+
     def close(self):
         if self.pg:
             self.td.destroy_process_group()
@@ -171,6 +184,33 @@ class Clocks:
         reasons = sorted({names[k] for r in rows for k in range(4) if r[3 + k] == "Active"})
         return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
                 "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_info():
+    """CPU model of the host and the thread settings the CPU arms use."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                model = line.split(":", 1)[1].strip()
+                if not model.isdigit():
+                    break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"cpu_model": model, "nproc": os.cpu_count(),
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS"),
+            "threads_used": os.cpu_count() or 1,
+            "threads_note": "the oracle's OpenMP loops run os.cpu_count() threads (num_threads "
+                            "passed explicitly; OMP_NUM_THREADS is not read)"}
 
 
 def measured_peaks():
@@ -266,20 +306,38 @@ def cpu_baseline(min_seconds=10.0, max_steps=50):
 
     threads = os.cpu_count() or 1
     st, n_amp, p = equilibrated_slab(threads)
-    O.md_step(p, st, nthreads=threads)  # warm-up
-    steps = 0
-    t0 = time.perf_counter()
-    while steps < max_steps:
-        O.md_step(p, st, nthreads=threads)
-        steps += 1
-        if time.perf_counter() - t0 >= min_seconds:
-            break
-    dt = time.perf_counter() - t0
     n = len(st["pos"])
-    return {"value": n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} MD steps (drift, density, force, bonded, kick) of one equilibrated "
-                      f"bilayer period of the workload (64x64x4.8, {n} beads, ~150 neighbours per "
-                      f"bead), FP64 C oracle, OpenMP"}
+    pairs = O.pair_count(p, st["pos"], threads) / n
+
+    def timed(fast):
+        O.use_fast_build(fast)
+        try:
+            O.md_step(p, st, nthreads=threads)  # warm-up
+            steps = 0
+            t0 = time.perf_counter()
+            while steps < max_steps:
+                O.md_step(p, st, nthreads=threads)
+                steps += 1
+                if time.perf_counter() - t0 >= min_seconds:
+                    break
+            return steps, time.perf_counter() - t0
+        finally:
+            O.use_fast_build(False)
+
+    steps, dt = timed(False)
+    steps_f, dt_f = timed(True)
+    out = {"value": n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+           "sample": f"{steps} MD steps (drift, density, force, bonded, kick) of one equilibrated "
+                     f"bilayer period of the workload (64x64x4.8, {n} beads, {pairs:.1f} ordered "
+                     f"pairs within the cutoff per bead), FP64 C oracle (-O2, no contraction), "
+                     f"OpenMP",
+           "pairs_per_bead": pairs,
+           "production_flags": {"value": n * steps_f / dt_f, "unit": "particle-steps/s",
+                                "steps": steps_f,
+                                "flags": "-O3 -ffast-math -funroll-loops (the reference's "
+                                         "Makefile:10,21-23)"}}
+    out.update(cpu_info())
+    return out
 
 
 def run_reference(args, rank, world, budget_s=90.0):
@@ -311,15 +369,18 @@ def run_reference(args, rank, world, budget_s=90.0):
     dt = time.perf_counter() - t0
     n = len(st["pos"])
     value = n * args.steps / dt
+    pairs = O.pair_count(p, st["pos"], threads) / n
     sample = (f"each step one MD step (drift, density, force, bonded, kick) of an equilibrated "
               f"bilayer patch of membrane_1m ({box[0]:g}x{box[1]:g}x{box[2]:g}, {n} beads, "
-              f"~150 neighbours per bead), FP64 C oracle of the reference algorithm, OpenMP")
+              f"{pairs:.1f} ordered pairs within the cutoff per bead), FP64 C oracle of the "
+              f"reference algorithm, OpenMP")
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "config": workload_desc(n, n_amp), "impl": "reference",
-           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
-                            "kind": "port", "sample": sample},
+           "cpu_baseline": dict({"value": value, "unit": "particle-steps/s", "cores": threads,
+                                 "kind": "port", "sample": sample, "pairs_per_bead": pairs},
+                                **cpu_info()),
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -366,7 +427,7 @@ def liquid_bench(steps=200, equil=300, device=0):
     particles), Warren form A = -40, B = 25, r_d = 0.75, sigma 3, dt 0.005,
     uniform random start. The FP32 engine (tuned over reach and skin) against
     the plain FP64 kernels of the same step, with the measured force error."""
-    from implicit_dpd_gb300.abi import CFG_FP64_PAIRS, FORM_WARREN
+    from implicit_dpd_gb300.abi import CFG_FP64_KEPT, CFG_FP64_PAIRS, FORM_WARREN
     from implicit_dpd_gb300.engine import Engine, derive_params
 
     box = np.array([55.0, 55.0, 55.0])
@@ -410,9 +471,23 @@ def liquid_bench(steps=200, equil=300, device=0):
     e64.step(10)
     v64 = n * 10 / (e64.last_step_ms() * 1e-3)
     e64.close()
+    # the engine's own algorithm in FP64 (kept lists at reach 1, each pair once)
+    ek = engine(CFG_FP64_KEPT, st_eq)
+    ek.density()
+    ek.force()
+    fk = ek.download()["acc"]
+    magk = np.linalg.norm(fk, axis=1)
+    errk = np.linalg.norm(f32 - fk, axis=1) / np.maximum(magk, np.sqrt(np.mean(magk ** 2)))
+    ek.set_tuning(1, skin)
+    ek.step(2)
+    ek.step(10)
+    vk = n * 10 / (ek.last_step_ms() * 1e-3)
+    ek.close()
     return {"workload": "mdpd_liquid_1m", "n_particles": int(n), "steps": steps,
             "equilibration_steps": equil, "tuning": {"reach": reach, "skin": skin},
             "value": v32, "fp64_plain": v64, "speedup_fp32_over_fp64": v32 / v64,
+            "fp64_same_algorithm": vk, "speedup_fp32_over_fp64_same_algorithm": v32 / vk,
+            "force_error_vs_fp64_same_algorithm": float(errk.max()),
             "unit": "particle-steps/s",
             "force_error": {"max_rel": float(err.max()),
                             "aggregate": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))},
@@ -420,27 +495,71 @@ def liquid_bench(steps=200, equil=300, device=0):
                            "sigma 3, dt 0.005, uniform random start"}
 
 
-def replicas_bench(steps=50, n_rep=256, device=0):
-    """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
-    A in [-50, -30], B = 25, densities 5-7): all replicas in one handle,
-    one CUDA graph per step, against the same replicas stepped one handle at
-    a time with the same (reach, skin), tuned on the batch. Returns
-    particle-steps/s of both."""
+def replica_params(reps):
+    """Warren-form parameters of the batched replicas (A per replica, B 25,
+    r_d 0.75, sigma 3, dt 0.005, each replica's own seed)."""
     from implicit_dpd_gb300.abi import FORM_WARREN
-    from implicit_dpd_gb300.engine import Engine, derive_params
+    from implicit_dpd_gb300.engine import derive_params
 
-    reps = configs.mdpd_replicas(n_rep)
     params = []
     for r in reps:
         p = derive_params(configs.run_param(r["box"], dt=0.005, cf_r=3.0))
         p.seed, p.time, p.form = r["seed"], 1, FORM_WARREN
         p.warren_a, p.warren_b, p.warren_rd = r["a"], 25.0, 0.75
         params.append(p)
-    n_tot = sum(len(r["state"]["pos"]) for r in reps)
-    eb = Engine(n_replicas=n_rep, device=device)
-    for k, (r, p) in enumerate(zip(reps, params)):
-        eb.set_params(p, k)
-        eb.upload(r["state"], k)
+    return params
+
+
+def replica_observables_cpu(reps, rank, world, dist, steps=3):
+    """The multi-rank replica path on the host: the replicas are dealt to the
+    ranks by LPT on their particle counts, each rank steps its own (CPU
+    oracle) and the per-replica kinetic temperatures are gathered in replica
+    order. Returns the gathered temperatures, the owner rank of every replica
+    and the replicas this rank stepped."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from implicit_dpd_gb300.partition import lpt_partition
+
+    sizes = [len(r["state"]["pos"]) for r in reps]
+    parts, _ = lpt_partition(sizes, world)
+    params = replica_params(reps)
+    mine = {}
+    for i in parts[rank]:
+        st = {k: np.array(v, copy=True) for k, v in reps[i]["state"].items()}
+        p = params[i]
+        for _ in range(steps):
+            O.md_step(p, st)
+        mine[i] = float((st["vel"] ** 2).sum() / (3.0 * len(st["vel"])))
+    temps = {}
+    for part in dist.gather(mine):
+        temps.update({int(k): v for k, v in part.items()})
+    owner = [next(k for k, p in enumerate(parts) if i in p) for i in range(len(reps))]
+    return {"temperature": [temps[i] for i in range(len(reps))], "owner": owner,
+            "stepped_here": sorted(parts[rank])}
+
+
+def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
+    """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
+    A in [-50, -30], B = 25, densities 5-7): all of a rank's replicas in one
+    handle, one CUDA graph per step, against the same replicas stepped one
+    handle at a time with the same (reach, skin), tuned on the batch. On
+    several ranks the replicas are dealt out by LPT on their particle counts
+    (no exchange while stepping); the job's rate is all particles x steps
+    over the slowest rank's time. Returns particle-steps/s of both forms."""
+    from implicit_dpd_gb300.engine import Engine
+    from implicit_dpd_gb300.partition import imbalance, lpt_partition
+
+    dist = dist or Dist(1)
+    reps = configs.mdpd_replicas(n_rep)
+    sizes = [len(r["state"]["pos"]) for r in reps]
+    parts, loads = lpt_partition(sizes, world)
+    mine = parts[rank]
+    params = replica_params(reps)
+    n_tot = sum(sizes)
+    eb = Engine(n_replicas=len(mine), device=device)
+    for k, i in enumerate(mine):
+        eb.set_params(params[i], k)
+        eb.upload(reps[i]["state"], k)
     eb.step(3)
     times = {}
     for reach, skin in [(1, 0.0), (1, 0.2), (1, 0.3)]:
@@ -451,23 +570,25 @@ def replicas_bench(steps=50, n_rep=256, device=0):
     reach, skin = min(times, key=times.get)
     eb.set_tuning(reach, skin)
     eb.step(3)
+    dist.barrier()
     eb.step(steps)
-    batched = n_tot * steps / (eb.last_step_ms() * 1e-3)
+    batched = n_tot * steps / (dist.max(eb.last_step_ms()) * 1e-3)
     eb.close()
     singles = []
-    for r, p in zip(reps, params):
+    for i in mine:
         e = Engine(device=device)
-        e.set_params(p)
-        e.upload(r["state"])
+        e.set_params(params[i])
+        e.upload(reps[i]["state"])
         e.set_tuning(reach, skin)
         e.step(3)
         singles.append(e)
     import torch
     torch.cuda.synchronize()
+    dist.barrier()
     t0 = time.perf_counter()
     for e in singles:  # one replica after the other, each its own graph launches
         e.step(steps)
-    t1 = time.perf_counter() - t0
+    t1 = dist.max(time.perf_counter() - t0)
     one_at_a_time = n_tot * steps / t1
     for e in singles:
         e.close()
@@ -475,9 +596,12 @@ def replicas_bench(steps=50, n_rep=256, device=0):
             "steps": steps, "tuning": {"reach": reach, "skin": skin},
             "batched": batched, "one_at_a_time": one_at_a_time,
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
+            "partition": {"ranks": world, "rule": "greedy LPT on particle counts",
+                          "replicas_per_rank": [len(p) for p in parts],
+                          "particles_per_rank": loads, "imbalance": imbalance(loads)},
             "description": "256 MDPD liquids (Warren form, A in [-50,-30], B 25, r_d 0.75, "
-                           "densities 5-7, 2k-60k particles log-uniform) in one handle and one "
-                           "graph per step vs one handle per replica stepped in turn"}
+                           "densities 5-7, 2k-60k particles log-uniform) in one handle per rank "
+                           "and one graph per step vs one handle per replica stepped in turn"}
 
 
 def save_state(path, e, n_amp, box, layers, tune):
@@ -533,9 +657,89 @@ def autotune(e, steps=40):
     return tune(e, steps=steps)
 
 
-def run_engine(args, rank, world, local_rank):
-    from implicit_dpd_gb300.abi import CFG_FP64_PAIRS
+def pair_roofline(kernel_ms, pairs, n, clocks, device):
+    """Roofline of the dominant pair pass against its own bound, CUDA-core
+    instruction issue: the algorithmic lane operations of the reference's
+    pair work (OPS_PER_ORDERED_PAIR x the ordered pairs within the cutoff,
+    counted on the device) over the kernel's CUDA-event time, against 4
+    warp-instruction issue slots x 32 lanes x SMs x the sampled SM clock.
+    The HBM figures and the ncu DRAM traffic of the same kernel ride along."""
+    import torch
 
+    top = max(PAIR_KERNELS, key=lambda k: kernel_ms[k])
+    kinfo = PAIR_KERNELS[top]
+    top_ms = kernel_ms[top]
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    ops = OPS_PER_ORDERED_PAIR[top] * pairs
+    achieved = ops / (top_ms * 1e-3) / 1e12
+    peak = 4.0 * 32.0 * sms * mhz * 1e6 / 1e12
+    hbm_peak, peak_kind = measured_peaks()
+    hbm = kinfo["bytes_per_particle"] * n / (top_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(kinfo["profile"])
+    return {"kernel": kinfo["kernel"], "bound": "issue", "achieved": achieved, "peak": peak,
+            "unit": "TOP/s", "frac": achieved / peak, "traffic": traffic,
+            "kernel_ms": top_ms, "ordered_pairs": pairs, "pairs_per_bead": pairs / n,
+            "ops_per_ordered_pair": OPS_PER_ORDERED_PAIR[top],
+            "definition": "achieved = ops_per_ordered_pair x ordered pairs within the cutoff "
+                          "(idpd_pair_count of the timed state) / the kernel's CUDA-event time; "
+                          "peak = 4 issue slots x 32 lanes x SMs x median sampled SM clock "
+                          f"({sms} SMs, {mhz:g} MHz); lane operations in 1e12/s",
+            "evaluated_pairs_frac": achieved / peak / 2.0,
+            "evaluated_pairs_note": "the engine evaluates each pair once (the reference twice): "
+                                    "against its own evaluations the fraction is half",
+            "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+                    "bytes_per_particle": kinfo["bytes_per_particle"],
+                    "peak_source": f"{peak_kind} copy bandwidth (of {peak_kind})",
+                    "traffic_over_algorithmic": (traffic / (kinfo["bytes_per_particle"] * n)
+                                                 if traffic else None)}}
+
+
+def fp64_arms(st64, n_amp, rp, tune, value32, steps, device):
+    """Both FP64 arms on one state: particle-steps/s, the FP32 engine's
+    speed-up over each, and the FP32 engine's pair-force error against each
+    (pair passes only, same positions)."""
+    from implicit_dpd_gb300.abi import CFG_FP64_KEPT, CFG_FP64_PAIRS
+
+    e32 = make_engine(st64, n_amp, rp, device=device)
+    e32.density()
+    e32.force()
+    f32 = e32.download()["acc"]
+    e32.close()
+
+    def arm(flags, kept):
+        e = make_engine(st64, n_amp, rp, flags=flags, device=device)
+        e.density()
+        e.force()
+        f64 = e.download()["acc"]
+        mag = np.linalg.norm(f64, axis=1)
+        floor = np.sqrt(np.mean(mag ** 2))
+        err = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, floor)
+        if kept:
+            e.set_tuning(1, tune["skin"])
+        e.step(2)
+        k = max(2, min(steps, 10))
+        e.step(k)
+        ms = e.last_step_ms()
+        e.close()
+        v = len(st64["pos"]) * k / (ms * 1e-3)
+        return {"value": v, "unit": "particle-steps/s", "steps": k, "ms_per_step": ms / k,
+                "speedup_fp32_over_fp64": value32 / v,
+                "force_error": {"max_rel": float(err.max()),
+                                "aggregate": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+                                "bar": 1e-5,
+                                "definition": "per particle |F32 - F64| / max(|F64|, rms |F64|), "
+                                              "pair forces of the timed state"}}
+
+    plain = arm(CFG_FP64_PAIRS, False)
+    plain["algorithm"] = "one thread per particle, 27 cells every step, each pair from both sides"
+    same = arm(CFG_FP64_KEPT, True)
+    same["algorithm"] = (f"the engine's: kept lists (reach 1, skin {tune['skin']:g}), each pair "
+                         "once by its owner, fixed-point sums; FP64 pair arithmetic")
+    return plain, same
+
+
+def run_engine(args, rank, world, local_rank):
     dist = Dist(world)
     box, layers = np.asarray(args.box, np.float64), args.layers
     st, n_amp, rp = workload(box=box, layers=layers)
@@ -568,69 +772,21 @@ def run_engine(args, rank, world, local_rank):
     value = n * args.steps * world / (ms_max * 1e-3)
 
     # per-kernel CUDA-event times of un-graphed steps (dominant kernel = force)
+    pairs = e.pair_count()  # ordered pairs within the cutoff of the last timed step
     prof = [e.profile_step() for _ in range(5)]
     kernel_ms = {k: statistics.median(p_[k] for p_ in prof) for k in prof[0]}
-    top = max(PAIR_KERNELS, key=lambda k: kernel_ms[k])
-    kinfo = PAIR_KERNELS[top]
-    top_ms = kernel_ms[top]
-    peak, peak_kind = measured_peaks()
-    achieved = kinfo["bytes_per_particle"] * n / (top_ms * 1e-3) / 1e9
-    roofline = {"kernel": kinfo["kernel"], "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profiled_traffic(kinfo["profile"]),
-                "peak_source": f"{peak_kind} copy bandwidth (of {peak_kind})",
-                "kernel_ms": top_ms, "bytes_per_particle": kinfo["bytes_per_particle"],
-                "note": "the pair passes are bound by CUDA-core instruction issue (distance "
-                        "tests, Saru hash, transcendentals per pair), not by HBM; the HBM "
-                        "fraction is small by construction"}
-    # the bound the pair passes do meet: warp-instruction issue (4 per SM and
-    # clock), with the kernel's instructions per bead from its ncu capture
-    ipb = profiled_inst_per_bead(kinfo["profile"])
-    if ipb is not None:
-        import torch
-
-        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
-        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
-        if mhz:
-            ach = ipb * n / (top_ms * 1e-3)
-            peak_i = 4.0 * sms * mhz * 1e6
-            roofline["issue"] = {
-                "achieved": ach, "peak": peak_i, "unit": "warp instructions/s", "frac": ach / peak_i,
-                "inst_per_particle": ipb,
-                "source": "smsp__inst_executed.sum per bead of the committed ncu capture x N / the "
-                          "kernel's CUDA-event time; peak = 4 issue slots x SMs x median SM clock"}
+    roofline = pair_roofline(kernel_ms, pairs, n, clocks, local_rank)
     step_gbs = STEP_BYTES_PER_PARTICLE * n / (ms_max / args.steps * 1e-3) / 1e9
 
-    # plain FP64 pair kernels on the same workload (the baseline of the metric)
-    fp64 = None
+    # the FP64 arms of the metric on the timed state: the plain FP64 kernels
+    # (one thread per particle, 27 cells, each pair from both sides) and the
+    # engine's own algorithm in FP64 (kept lists, each pair once)
+    fp64, fp64_same = None, None
     if not args.no_fp64:
         eq = e.download()
         st64 = dict(st, pos=eq["pos"], vel=eq["vel"], acc=eq["acc"])
-        e64 = make_engine(st64, n_amp, rp, flags=CFG_FP64_PAIRS, device=local_rank)
-        # the stated force error: both pair passes on the timed state, FP32
-        # engine against the plain FP64 kernels
-        e32 = make_engine(st64, n_amp, rp, device=local_rank)
-        for x in (e32, e64):
-            x.density()
-            x.force()
-        f32, f64 = e32.download()["acc"], e64.download()["acc"]
-        e32.close()
-        mag = np.linalg.norm(f64, axis=1)
-        floor = np.sqrt(np.mean(mag ** 2))
-        err = np.linalg.norm(f32 - f64, axis=1) / np.maximum(mag, floor)
-        force_err = {"max_rel": float(err.max()),
-                     "aggregate": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
-                     "bar": 1e-5,
-                     "definition": "per particle |F32 - F64| / max(|F64|, rms |F64|), pair "
-                                   "forces of the timed state, plain FP64 kernels as reference"}
-        e64.step(1)
-        k64 = max(2, min(args.steps, 10))
-        e64.step(k64)
-        ms64 = e64.last_step_ms()
-        v64 = n * k64 / (ms64 * 1e-3)
-        fp64 = {"value": v64, "unit": "particle-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
-                "speedup_fp32_over_fp64": value / world / v64, "force_error": force_err}
-        e64.close()
+        fp64, fp64_same = fp64_arms(st64, n_amp, rp, reach, value / world, args.steps,
+                                    local_rank)
 
     # end to end through the C ABI: host pinned pos/vel/acc in, one step, out
     e2e = None
@@ -651,7 +807,8 @@ def run_engine(args, rank, world, local_rank):
                "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": k2,
                "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state per step"}
 
-    batched = replicas_bench(device=local_rank) if not args.no_replicas else None
+    batched = (replicas_bench(device=local_rank, rank=rank, world=world, dist=dist)
+               if not args.no_replicas else None)
     reaction = reaction_bench(reach, device=local_rank) if not args.no_reaction else None
     liquid = liquid_bench(device=local_rank) if not args.no_liquid else None
     cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
@@ -665,7 +822,8 @@ def run_engine(args, rank, world, local_rank):
                                                list_rebuilds_in_timed_steps=rebuilds,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
-           "kernel_ms": kernel_ms, "fp64_plain": fp64, "e2e": e2e, "cpu_baseline": cpu,
+           "kernel_ms": kernel_ms, "fp64_plain": fp64, "fp64_same_algorithm": fp64_same,
+           "e2e": e2e, "cpu_baseline": cpu,
            "batched_replicas": batched, "reaction": reaction, "liquid": liquid,
            "gpu_launches": args.steps * (KERNELS_PER_KEPT_STEP if reach["skin"] > 0 else KERNELS_PER_STEP)
                            + n_reorders * KERNELS_PER_REORDER,

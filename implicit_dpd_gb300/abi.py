@@ -21,6 +21,7 @@ STATUS_NAMES = {
 }
 
 CFG_FP64_PAIRS = 0x1
+CFG_FP64_KEPT = 0x4
 CFG_TIMING = 0x2
 
 NONE32 = 0xFFFFFFFF  # amp_id / unit of solvent beads (parameter.hpp:450-451)
@@ -129,6 +130,10 @@ class IdpdChemInfo(C.Structure):
         ("stopped", C.c_int32),
         ("amp_num", C.c_uint32),
         ("core_raw", (C.c_double * 9) * CHEM_MAX_CORE),
+        ("n_core", C.c_int32),
+        ("reserved", C.c_int32),
+        ("h2t", (C.c_double * 3) * CHEM_MAX_CORE),
+        ("core_h", (C.c_double * 3) * CHEM_MAX_CORE),
     ]
 
 
@@ -144,7 +149,8 @@ class IdpdConfig(C.Structure):
 
 
 class IdpdTuning(C.Structure):
-    _fields_ = [("reach", C.c_int32), ("skin", C.c_float), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("reach", C.c_int32), ("skin", C.c_float), ("pair_lanes", C.c_int32),
+                ("pair_blocks", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class IdpdPrecursor(C.Structure):

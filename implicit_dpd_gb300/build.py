@@ -16,7 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libidpd_engine.so")
-SOURCES = ["engine.cu", "kernels_cells.cu", "kernels_pairs.cu", "kernels_integrate.cu",
+SOURCES = ["engine.cu", "kernels_cells.cu", "kernels_pairs.cu", "kernels_force.cu",
+           "kernels_integrate.cu",
            "kernels_chem.cu", "kernels_walks.cu", "no_alloc.cu", "formats.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

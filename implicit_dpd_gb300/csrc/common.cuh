@@ -117,16 +117,15 @@ struct Saru {
 
 // Normal deviate of Saru::nrml() (saruprng.hpp:442-445) in FP32:
 // sqrt(-2 ln u1) cos(2 pi u2) with u = (2 (draw >> 1) + 1) / 2^32.
-// -ln u1 is taken from the exact complement 1 - u1 when u1 >= 1/2, so it
-// keeps its relative accuracy as u1 -> 1.
 //
-// Both factors are evaluated without branches (lanes of a warp take
-// different ends of the interval):
-//  * u1 < 1/2: -ln u1 = -log2(u1) ln 2 with the hardware log2, whose error is
-//    below 2 ulp of |log2 u1| >= 1;
-//  * u1 >= 1/2: c = 1 - u1 comes exactly from the integer complement and
-//    -ln(1 - c) = 2 atanh(z), z = c / (2 - c) <= 1/3, from its Taylor series
-//    z + z^3/3 + ... + z^15/15 (truncation below 1e-8 relative);
+// One logarithm per draw, by the same branch-free arithmetic on every lane:
+//  * u1 = m1 2^-32 = f' 2^-j with f' in [1/sqrt 2, sqrt 2): j = clz(m1),
+//    M = m1 << j in [2^31, 2^32) gives f = M 2^-32 in [1/2, 1), and f is
+//    doubled (j + 1) when below 1/sqrt 2;
+//  * c = 1 - f' is exact in integers: (2^32 - M) 2^-32, or (2^32 - 2M) 2^-32
+//    when doubled, so -ln u1 keeps its relative accuracy as u1 -> 1;
+//  * -ln u1 = j ln 2 + 2 atanh(z), z = c / (2 - c), |z| <= 0.1716, with the
+//    Taylor series z + z^3/3 + ... + z^9/9 (truncation below 3e-9 relative);
 //  * cos(2 pi u2) = cos(2 pi (u2 - 1)): the draw read as a signed integer
 //    gives the argument in [-pi, pi), where the hardware cosine's absolute
 //    error is below 2^-21.4 (the deviate's error stays below 2.4e-6 for the
@@ -135,20 +134,19 @@ __device__ __forceinline__ float saru_nrml_f32(Saru& s) {
   const uint32_t m1 = s.next() | 1u;  // 2 (draw >> 1) + 1 = u1 * 2^32
   const uint32_t m2 = s.next() | 1u;  // u2 * 2^32
   const float two_m32 = 2.3283064365386963e-10f;  // 2^-32
-  const float la = -__log2f(__uint2float_rn(m1) * two_m32) * 0.69314718055994531f;
-  const float c = __uint2float_rn(0u - m1) * two_m32;  // 1 - u1, exact complement
+  const int j = __clz(m1);
+  const uint32_t M = m1 << j;
+  const int dbl = M < 0xB504F334u ? 1 : 0;  // f < 1/sqrt 2 (0xB504F334 = 2^32 / sqrt 2)
+  const uint32_t Md = M << dbl;             // f' 2^32, modulo 2^32 when doubled
+  const float c = __int2float_rn((int)(0u - Md)) * two_m32;  // 1 - f'
   const float z = __fdividef(c, 2.0f - c);
   const float z2 = z * z;
-  float p = 1.0f / 15.0f;
-  p = fmaf(p, z2, 1.0f / 13.0f);
-  p = fmaf(p, z2, 1.0f / 11.0f);
-  p = fmaf(p, z2, 1.0f / 9.0f);
+  float p = 1.0f / 9.0f;
   p = fmaf(p, z2, 1.0f / 7.0f);
   p = fmaf(p, z2, 1.0f / 5.0f);
   p = fmaf(p, z2, 1.0f / 3.0f);
   p = fmaf(p, z2, 1.0f);
-  const float lb = 2.0f * z * p;
-  const float nlog = m1 < 0x80000000u ? la : lb;
+  const float nlog = fmaf(__int2float_rn(j + dbl), 0.69314718055994531f, 2.0f * (z * p));
   // cos(2 pi u2) = cos(2 pi (u2 - 1)): the signed draw gives the argument in [-pi, pi)
   const float cs = __cosf(__int2float_rn((int)m2) * (6.28318530717958647692f * two_m32));
   const float r2 = 2.0f * nlog;

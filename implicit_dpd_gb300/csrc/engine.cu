@@ -68,7 +68,7 @@ struct idpd_handle {
   cudaGraphExec_t graph = nullptr;
   int steps_since_sort = 0;
   float last_ms = 0.f;
-  PairTuning tune{1, 0.0f};
+  PairTuning tune{1, 0.0f, 16, 1};
   bool vl_dirty = true;                 // cells rebuilt outside the step: the kept lists are stale
   std::string err;
   // chemistry (replica 0 of a one-replica handle)
@@ -91,6 +91,8 @@ struct idpd_handle {
   ObsBuffers obs_buf{};                 // per-layout scratch (null until needed)
   cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
   WalkState* walks = nullptr;           // FDPS multi-walk buffers (created on first use)
+  unsigned long long* pair_sum = nullptr;  // device word of idpd_pair_count
+  bool pairs_valid = false;             // a density pass has run on the current layout
 };
 
 namespace {
@@ -287,9 +289,7 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.scan_part, (cc + 4095) / 4096 + 1);
   AL(d.perm, cap); AL(d.rank, cap); AL(d.scell, cap);
   AL(d.posf, cap); AL(d.velf, cap); AL(d.densf, cap); AL(d.poslo, cap);
-  AL(d.fqx, 3 * (size_t)cap);
-  d.fqy = d.fqx + cap;
-  d.fqz = d.fqx + 2 * (size_t)cap;
+  AL(d.fq, 4 * (size_t)cap);
   AL(d.nbl, (size_t)kNbrCap * cap); AL(d.nbn, cap);
   AL(d.dsum, 4 * (size_t)cap);
   AL(d.topol, 4 * ac);
@@ -300,16 +300,20 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.blk_rep, bc);
   AL(d.blk_row, bc);
   AL(d.blk_part, 3 * bc);
+  AL(d.npair, cap);
+  AL(h->pair_sum, 1);
   AL(d.rep_mean, 3 * h->R);
   AL(d.err, 1);
   AL(h->amp_rep, ac);
-  if (h->flags & IDPD_CFG_FP64_PAIRS) { AL(d.dens64, 3 * (size_t)cap); }
+  if (h->flags & (IDPD_CFG_FP64_PAIRS | IDPD_CFG_FP64_KEPT)) { AL(d.dens64, 3 * (size_t)cap); }
+  if (h->flags & IDPD_CFG_FP64_KEPT) { AL(d.svel, 4 * (size_t)cap); }
 #undef AL
-  d.pqx = d.pqy = d.pqz = nullptr;
+  d.pq = nullptr;
   d.dqx = d.dqy = d.dqz = nullptr;
   CK(cudaMemsetAsync(d.cell_cnt, 0, sizeof(int) * cc, h->st));
   CK(cudaMemsetAsync(d.err, 0, sizeof(int), h->st));
   CK(cudaMemsetAsync(d.dsum, 0, sizeof(unsigned long long) * 4 * (size_t)cap, h->st));
+  CK(cudaMemsetAsync(d.npair, 0, sizeof(uint32_t) * (size_t)cap, h->st));
   h->cap = cap;
   h->ncell_cap = cc;
   h->nblk_cap = bc;
@@ -319,12 +323,10 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
 
 // Per-particle virial of the pair pass (fine-grained API and observation).
 int ensure_press(idpd_handle* h) {
-  if (h->d.pqx) return IDPD_OK;
+  if (h->d.pq) return IDPD_OK;
   int rc;
   DevState& d = h->d;
-  if ((rc = dalloc(h, &d.pqx, 3 * (size_t)h->cap))) return rc;
-  d.pqy = d.pqx + h->cap;
-  d.pqz = d.pqx + 2 * (size_t)h->cap;
+  if ((rc = dalloc(h, &d.pq, 4 * (size_t)h->cap))) return rc;
   invalidate_graph(h);
   return IDPD_OK;
 }
@@ -467,6 +469,7 @@ int commit(idpd_handle* h) {
   for (int r = 0; r < h->R; r++)
     if (!h->params_set[r]) return fail(h, IDPD_ERR_STATE, "replica %d has no parameters", r);
   if (h->layout_dirty) {
+    h->pairs_valid = false;
     invalidate_graph(h);
     h->reps_h.assign(h->R, RepDev{});
     int row = 0, cell = 0, blk = 0, amp = 0;
@@ -652,6 +655,13 @@ int check_device_error(idpd_handle* h) {
   }
 }
 
+// Arithmetic of the pair passes chosen at creation.
+int pair_mode(const idpd_handle* h) {
+  if (h->flags & IDPD_CFG_FP64_PAIRS) return kPairsF64;
+  if (h->flags & IDPD_CFG_FP64_KEPT) return kPairsF64Kept;
+  return kPairsF32;
+}
+
 // Cell list over the current positions (no drift).
 void enqueue_cells(idpd_handle* h, bool drift) {
   h->vl_dirty = true;
@@ -664,10 +674,10 @@ void enqueue_cells(idpd_handle* h, bool drift) {
 // the observation kernels (the records are written only for replicas whose
 // step counter is due).
 void enqueue_step(idpd_handle* h, bool observe) {
-  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  const int mode = pair_mode(h);
   DevState d = h->d;  // the step writes no fine-grained side outputs
   d.dqx = d.dqy = d.dqz = nullptr;
-  const bool verlet = d.vdev && h->tune.skin > 0.0f && !fp64;
+  const bool verlet = d.vdev && h->tune.skin > 0.0f && mode != kPairsF64;
   if (verlet) {  // cells and lists only on rebuild steps
     const int* gate = &d.vdev->rebuild;
     launch_drift_disp(d, h->nblk, h->st);
@@ -675,17 +685,18 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_bin_gated(d, h->nblk, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
-    launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
+    launch_verlet_build(d, h->ncell_tot, h->R, h->tune.reach, h->st);
   } else {
     launch_drift_bin(d, h->nblk, true, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
-  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, h->prec_any && d.phit, h->cap, h->st);
-  launch_force(d, h->nblk, fp64, observe, verlet, h->tune, form_mask(h), h->cap, h->st);
+  const bool marks = mode == kPairsF32 && h->prec_any && d.phit;
+  launch_density(d, h->nblk, mode, h->tune.reach, verlet, marks, h->cap, h->st);
+  launch_force(d, h->nblk, mode, observe, verlet, h->tune, form_mask(h), h->cap, h->st);
   if (h->prec_any) {
     d.prec_count = h->prec_dev;
-    launch_precursor(d, h->nblk, !fp64, h->st);
+    launch_precursor(d, h->nblk, marks, h->st);
   }
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
@@ -812,6 +823,9 @@ int idpd_create(const idpd_config* cfg, idpd_handle** out) {
   if (!cfg || !out) return fail(nullptr, IDPD_ERR_INVALID_ARG, "null pointer");
   *out = nullptr;
   if (cfg->n_replicas < 1) return fail(nullptr, IDPD_ERR_INVALID_ARG, "n_replicas must be >= 1");
+  if ((cfg->flags & IDPD_CFG_FP64_PAIRS) && (cfg->flags & IDPD_CFG_FP64_KEPT))
+    return fail(nullptr, IDPD_ERR_INVALID_ARG,
+                "IDPD_CFG_FP64_PAIRS and IDPD_CFG_FP64_KEPT exclude each other");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -1102,7 +1116,20 @@ int idpd_download_aux(idpd_handle* h, int32_t r, double* density, double* press,
       for (int k = 0; k < w; k++)
         out[(size_t)w * (orig[q] - (uint32_t)R.row_off) + k] = src[(size_t)w * q + k];
   };
-  if (density) {
+  if (density && h->density_valid && h->d.dens64 && pair_mode(h) != kPairsF32) {
+    // the FP64 arms: their FP64 densities (sorted order), unrounded
+    std::vector<double> ds(3 * (size_t)n);
+    CK(cudaMemcpyAsync(perm.data(), h->d.perm + R.row_off, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(ds.data(), h->d.dens64 + 3 * (size_t)R.row_off, sizeof(double) * 3 * n,
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    std::vector<double> byrow(3 * (size_t)n);
+    for (int sidx = 0; sidx < n; sidx++) {
+      const int row = (int)perm[sidx] - R.row_off;
+      for (int k = 0; k < 3; k++) byrow[3 * (size_t)row + k] = ds[3 * (size_t)sidx + k];
+    }
+    scatter3(byrow, density, 3);
+  } else if (density) {
     if (!h->density_valid || !h->d.dqx) return fail(h, IDPD_ERR_STATE, "run idpd_density first");
     std::vector<long long> q[3];
     const long long* src[3] = {h->d.dqx, h->d.dqy, h->d.dqz};
@@ -1167,11 +1194,11 @@ int idpd_density(idpd_handle* h) {
   int rc = commit(h);
   if (rc) return rc;
   if ((rc = ensure_aux(h))) return rc;
-  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
   enqueue_cells(h, false);
-  launch_density(h->d, h->nblk, fp64, h->tune.reach, false, false, h->cap, h->st);
+  launch_density(h->d, h->nblk, pair_mode(h), h->tune.reach, false, false, h->cap, h->st);
   launch_com(h->d, h->nblk, h->cm64, h->cm_cnt, h->st);
   h->density_valid = true;
+  h->pairs_valid = true;
   return check_device_error(h);
 }
 
@@ -1182,8 +1209,7 @@ int idpd_force(idpd_handle* h) {
   if (rc) return rc;
   if (!h->density_valid) return fail(h, IDPD_ERR_STATE, "idpd_force needs idpd_density on the same positions");
   if ((rc = ensure_aux(h))) return rc;
-  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
-  launch_force(h->d, h->nblk, fp64, true, false, h->tune, form_mask(h), h->cap, h->st);
+  launch_force(h->d, h->nblk, pair_mode(h), true, false, h->tune, form_mask(h), h->cap, h->st);
   launch_fq_to_acc(h->d, h->nblk, h->press64, h->st);
   return check_device_error(h);
 }
@@ -1239,6 +1265,7 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   int rc = commit(h);
   if (rc) return rc;
   if (h->n_tot == 0 || nsteps == 0) return IDPD_OK;
+  h->pairs_valid = true;
   if (h->chem_on && h->chem_stopped)
     return fail(h, IDPD_ERR_STATE, "the reaction reached max_amp_num: the run has ended");
   if ((rc = ensure_verlet_ready(h)) || (rc = ensure_phit(h))) return rc;
@@ -1256,7 +1283,11 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     enqueue_step(h, variant == 1);
-    CK(cudaStreamEndCapture(h->st, &g));
+    const cudaError_t launch_err = cudaGetLastError();  // a launch refused during capture
+    const cudaError_t cap_err = cudaStreamEndCapture(h->st, &g);
+    if (cap_err != cudaSuccess || launch_err != cudaSuccess)
+      return fail(h, IDPD_ERR_CUDA, "step capture: %s (first launch error: %s)",
+                  cudaGetErrorString(cap_err), cudaGetErrorString(launch_err));
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
@@ -1301,6 +1332,12 @@ int idpd_sync(idpd_handle* h) {
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
   if (!h || !t) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
   if (t->reach < 1 || t->reach > 2) return fail(h, IDPD_ERR_INVALID_ARG, "reach must be 1 or 2");
+  if (t->reach != 1 && (h->flags & IDPD_CFG_FP64_KEPT))
+    return fail(h, IDPD_ERR_INVALID_ARG, "the FP64 engine-algorithm arm runs at reach 1");
+  if (t->pair_lanes != 0 && t->pair_lanes != 8 && t->pair_lanes != 16 && t->pair_lanes != 32)
+    return fail(h, IDPD_ERR_INVALID_ARG, "pair_lanes must be 8, 16 or 32 (0: 16)");
+  if (t->pair_blocks != 0 && t->pair_blocks != 1 && t->pair_blocks != 2 && t->pair_blocks != 4)
+    return fail(h, IDPD_ERR_INVALID_ARG, "pair_blocks must be 1, 2 or 4 (0: 1)");
   if (!(t->skin >= 0.0f && t->skin < 1.0f))
     return fail(h, IDPD_ERR_INVALID_ARG, "skin must be in [0, 1)");
   for (int r = 0; r < h->R; r++)
@@ -1311,6 +1348,10 @@ int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
                     (double)t->skin, 3.0 * (1.0 + t->skin));
   cudaSetDevice(h->device);
   const bool changed = t->reach != h->tune.reach || t->skin != h->tune.skin;
+  const int lanes = t->pair_lanes ? t->pair_lanes : 16, fblk = t->pair_blocks ? t->pair_blocks : 1;
+  if (lanes != h->tune.lanes || fblk != h->tune.fblk) invalidate_graph(h);
+  h->tune.lanes = lanes;
+  h->tune.fblk = fblk;
   h->tune.reach = t->reach;
   h->tune.skin = t->skin;
   if (changed && h->on_device && !h->layout_dirty) {
@@ -1327,6 +1368,8 @@ int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t) {
   std::memset(t, 0, sizeof(*t));
   t->reach = h->tune.reach;
   t->skin = h->tune.skin;
+  t->pair_lanes = h->tune.lanes;
+  t->pair_blocks = h->tune.fblk;
   return IDPD_OK;
 }
 
@@ -1342,6 +1385,21 @@ int idpd_list_rebuilds(idpd_handle* h, uint64_t* rebuilds) {
   return check_device_error(h);
 }
 
+int idpd_pair_count(idpd_handle* h, int32_t replica, uint64_t* ordered_pairs) {
+  if (!h || !ordered_pairs) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
+  if (replica < 0 || replica >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", replica);
+  *ordered_pairs = 0;
+  if (!h->on_device || !h->pairs_valid) return IDPD_OK;
+  cudaSetDevice(h->device);
+  const RepDev& R = h->reps_h[replica];
+  unsigned long long sum = 0;
+  launch_sum_pairs(h->d.npair, R.row_off, R.n, h->pair_sum, h->st);
+  CK(cudaMemcpyAsync(&sum, h->pair_sum, sizeof(sum), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  *ordered_pairs = sum;
+  return check_device_error(h);
+}
+
 int idpd_last_step_ms(const idpd_handle* h, float* ms) {
   if (!h || !ms) return IDPD_ERR_INVALID_ARG;
   *ms = h->last_ms;
@@ -1354,7 +1412,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   cudaSetDevice(h->device);
   int rc = commit(h);
   if (rc) return rc;
-  const bool fp64 = (h->flags & IDPD_CFG_FP64_PAIRS) != 0;
+  const int mode = pair_mode(h);
   std::vector<cudaEvent_t> ev(10);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   const char* nm[9] = {"drift_bin", "scan", "scatter_sort_pack", "list_build", "density",
@@ -1363,7 +1421,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   if (rc2) return rc2;
   DevState d = h->d;
   d.dqx = d.dqy = d.dqz = nullptr;
-  const bool verlet = d.vdev && h->tune.skin > 0.0f && !fp64;
+  const bool verlet = d.vdev && h->tune.skin > 0.0f && mode != kPairsF64;
   const int* gate = verlet ? &d.vdev->rebuild : nullptr;
   CK(cudaEventRecord(ev[0], h->st));
   if (verlet) {
@@ -1378,11 +1436,12 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
   CK(cudaEventRecord(ev[3], h->st));
-  if (verlet) launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
+  if (verlet) launch_verlet_build(d, h->ncell_tot, h->R, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
-  launch_density(d, h->nblk, fp64, h->tune.reach, verlet, false, h->cap, h->st);
+  h->pairs_valid = true;
+  launch_density(d, h->nblk, mode, h->tune.reach, verlet, false, h->cap, h->st);
   CK(cudaEventRecord(ev[5], h->st));
-  launch_force(d, h->nblk, fp64, false, verlet, h->tune, form_mask(h), h->cap, h->st);
+  launch_force(d, h->nblk, mode, false, verlet, h->tune, form_mask(h), h->cap, h->st);
   CK(cudaEventRecord(ev[6], h->st));
   launch_bonded_kick(d, h->nblk, true, h->st);
   CK(cudaEventRecord(ev[7], h->st));
@@ -1738,6 +1797,12 @@ int idpd_chem_get_info(idpd_handle* h, int32_t r, idpd_chem_info* info, uint32_t
   info->amp_num = c.amp_num;
   for (int k = 0; k < IDPD_CHEM_MAX_CORE && k < kChemMaxCore; k++)
     for (int q = 0; q < 9; q++) info->core_raw[k][q] = c.core_raw[k][q];
+  info->n_core = c.events > 0 ? c.n_core : 0;
+  for (int k = 0; k < info->n_core && k < IDPD_CHEM_MAX_CORE; k++)
+    for (int q = 0; q < 3; q++) {
+      info->h2t[k][q] = c.core_n[k][q];
+      info->core_h[k][q] = c.core_h[k][q];
+    }
   const int nt = std::min(c.n_targets, cap);
   if (targets && nt > 0 && h->chem_buf.targets) {
     CK(cudaMemcpyAsync(targets, h->chem_buf.targets, sizeof(uint32_t) * 2 * nt,

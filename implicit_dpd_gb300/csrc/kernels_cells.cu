@@ -340,6 +340,12 @@ __global__ void __launch_bounds__(kRowBlock) k_pack(DevState d, const int* gate)
   d.poslo[s] = make_float4(ex, ey, ez, 0.0f);
   d.velf[s] = make_float4(__double2float_rn(d.vx[i]), __double2float_rn(d.vy[i]),
                           __double2float_rn(d.vz[i]), __uint_as_float(d.id[i]));
+  if (d.svel) {  // FP64 engine-algorithm arm
+    double* v = d.svel + 4 * (size_t)s;
+    v[0] = d.vx[i];
+    v[1] = d.vy[i];
+    v[2] = d.vz[i];
+  }
 }
 
 void launch_scan_raw(int* cnt, int* start, int* part, int ncell, int n_tot, cudaStream_t st) {

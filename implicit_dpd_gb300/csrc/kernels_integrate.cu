@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(kRowBlock) k_bonded_kick(DevState d) {
   const RepDev* R = d.reps + r;
   if (i >= R->row_off + R->n) return;
   const int s = (int)d.rank[i];
-  long long f[3] = {d.fqx[s], d.fqy[s], d.fqz[s]};
+  const long long* fs = d.fq + 4 * (size_t)s;
+  long long f[3] = {fs[0], fs[1], fs[2]};
   const uint32_t a = d.amp_id[i];
   if (a != kNone && R->n_amp > 0) {
     const int u = (int)d.unit[i];
@@ -196,13 +197,15 @@ __global__ void __launch_bounds__(kRowBlock) k_fq_to_acc(DevState d, double* pre
   const RepDev* R = d.reps + r;
   if (s >= R->row_off + R->n) return;
   const uint32_t i = d.perm[s];
-  d.ax[i] = (double)d.fqx[s] * kForceUnscale;
-  d.ay[i] = (double)d.fqy[s] * kForceUnscale;
-  d.az[i] = (double)d.fqz[s] * kForceUnscale;
+  const long long* fs = d.fq + 4 * (size_t)s;
+  d.ax[i] = (double)fs[0] * kForceUnscale;
+  d.ay[i] = (double)fs[1] * kForceUnscale;
+  d.az[i] = (double)fs[2] * kForceUnscale;
   if (press) {
-    press[3 * i] = (double)d.pqx[s] * kForceUnscale;
-    press[3 * i + 1] = (double)d.pqy[s] * kForceUnscale;
-    press[3 * i + 2] = (double)d.pqz[s] * kForceUnscale;
+    const long long* ps = d.pq + 4 * (size_t)s;
+    press[3 * i] = (double)ps[0] * kForceUnscale;
+    press[3 * i + 1] = (double)ps[1] * kForceUnscale;
+    press[3 * i + 2] = (double)ps[2] * kForceUnscale;
   }
 }
 
@@ -437,9 +440,10 @@ __global__ void __launch_bounds__(kRowBlock) k_obs_rows(DevState d, ObsBuffers b
     // in this step start with press 0, chemmanager.hpp:59)
     const int s = (int)d.rank[i];
     if (s < d.cell_start[R->cell_off + R->ncell]) {
-      q[0] = d.pqx[s];
-      q[1] = d.pqy[s];
-      q[2] = d.pqz[s];
+      const long long* ps = d.pq + 4 * (size_t)s;
+      q[0] = ps[0];
+      q[1] = ps[1];
+      q[2] = ps[2];
     }
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

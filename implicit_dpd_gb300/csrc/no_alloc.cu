@@ -3,14 +3,15 @@
 // callers that must not allocate device memory: a host code whose own pool
 // owns the device budget, or a step loop in which the device-wide
 // synchronisation of cudaMalloc / cudaFree would stall the other streams.
-// The result equals idpd_cell_order's for the same rows (one grid of
-// floor(box) cells per axis, rows of a cell in ascending row order).
+// The grid is floor(box) cells per axis (cells of the pair cutoff 1.0), rows
+// of a cell in ascending row order: idpd_cell_order's result for the same
+// rows at the engine's default tuning (cell reach 1, skin 0). Other tunings
+// give idpd_cell_order other grids (floor(box / (1 + skin)) * reach cells).
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
-#include <mutex>
 
 #include "idpd_engine.h"
 #include "state.cuh"
@@ -34,12 +35,8 @@ static_assert(kScratchWords * 4 == IDPD_NOALLOC_SCRATCH_BYTES, "scratch size out
 static_assert(kOffCnt % 64 == 0 && kOffStart % 64 == 0 && kOffPart % 64 == 0, "alignment");
 
 // The scratch. Host code may not use this name as an address; the device
-// address comes from cudaGetSymbolAddress, once per device.
+// address comes from cudaGetSymbolAddress in the caller's current context.
 static __device__ __align__(256) uint32_t g_scratch[kScratchWords];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-uint32_t* g_addr[kMaxDevices] = {};
 
 int noalloc_fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -90,22 +87,17 @@ extern "C" int idpd_cell_order_noalloc(const double* pos, int32_t n, const doubl
   if (e != cudaSuccess)
     return noalloc_fail(IDPD_ERR_NO_DEVICE, "cell_order_noalloc: cudaGetDevice: %s",
                         cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return noalloc_fail(IDPD_ERR_INVALID_ARG, "cell_order_noalloc: device %d not supported", dev);
-  uint32_t* base;
-  {
-    // Set-up on the first call per device, with that device current.
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_scratch);
-      if (e != cudaSuccess)
-        return noalloc_fail(IDPD_ERR_CUDA, "cell_order_noalloc: cudaGetSymbolAddress: %s",
-                            cudaGetErrorString(e));
-      g_addr[dev] = (uint32_t*)p;
-    }
-    base = g_addr[dev];
-  }
+  // The scratch's device address in the context current on this thread,
+  // looked up on every call: no address is kept across calls, so a caller
+  // that switches contexts, or a device reset by any library of the process,
+  // cannot leave a stale address behind. The lookup allocates nothing; the
+  // first call on a device also loads this library's device code there (set-up).
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess)
+    return noalloc_fail(IDPD_ERR_CUDA, "cell_order_noalloc: cudaGetSymbolAddress on device %d: %s",
+                        dev, cudaGetErrorString(e));
+  uint32_t* base = (uint32_t*)p;
   cudaStream_t st = (cudaStream_t)stream;
   uint32_t* slot = base + kOffSlot;
   int* cnt = (int*)(base + kOffCnt);

@@ -6,7 +6,8 @@
 //   sorted order (rows grouped by cell, rebuilt every step):
 //     perm (sorted -> storage), rank (storage -> sorted), scell (global cell),
 //     float4 posf (cell-local position, prop bits), velf (velocity, id bits),
-//     densf (partial densities), int64 fixed-point pair force fq[3];
+//     densf (partial densities), int64 fixed-point pair force fq (x, y, z and
+//     a pad word per row: the three sums of a row share one 32-byte sector);
 //   cells: per-cell count and start (exclusive prefix) over all replicas.
 #pragma once
 
@@ -43,10 +44,11 @@ struct DevState {
   float4* poslo;               // low-order parts of the cell-local position
   uint32_t* nbl;               // [N * kNbrCap] in-range neighbours of pass 1 (sorted order)
   uint16_t* nbn;               // [N] list length (owned pairs), or 0xffff when it overflowed
-  long long *fqx, *fqy, *fqz;  // pair force, 2^-26 fixed point (one block of 3 x capacity)
-  long long *pqx, *pqy, *pqz;  // per-particle virial (fine-grained API, observation; one block)
+  long long* fq;               // [4N] pair force, 2^-26 fixed point: x, y, z, pad per sorted row
+  long long* pq;               // [4N] per-particle virial, same layout (fine-grained API, observation)
   long long *dqx, *dqy, *dqz;  // partial densities in RepDev::dens_unscale units (fine-grained API only)
-  double* dens64;              // [3N] partial densities of the plain FP64 arm (sorted order)
+  double* dens64;              // [3N] partial densities of the FP64 arms (sorted order)
+  double* svel;                // [4N] FP64 velocity per sorted row (FP64 engine-algorithm arm)
   unsigned long long* dsum;    // [4N] pass-1 partial densities by property, fixed point (zero between passes)
   // ---- topology
   uint32_t* topol;  // [4 * total molecules] storage rows
@@ -59,6 +61,8 @@ struct DevState {
   int* blk_row;
   // ---- reductions
   double* blk_part;  // [n_blocks * 3]
+  uint32_t* npair;   // [N] ordered pairs within the cutoff (r < 1, i != j) of each sorted row,
+                     // counted by pass 1 (2 x the owned pairs in the once-per-pair passes)
   double* rep_mean;  // [R * 3]
   int* err;          // device error word (0 = ok)
   unsigned long long* prec_count;  // [R] precursor conversions per replica
@@ -152,25 +156,36 @@ void launch_scatter_rows(const uint32_t* cell, const uint32_t* slot, const int* 
 void set_library_error(const char* msg);
 
 // kernels_pairs.cu
+// Arithmetic of the pair passes: the FP32 engine, the plain FP64 kernels
+// (IDPD_CFG_FP64_PAIRS) or the engine's algorithm in FP64 (IDPD_CFG_FP64_KEPT).
+enum PairMode : int { kPairsF32 = 0, kPairsF64 = 1, kPairsF64Kept = 2 };
 struct PairTuning {
   int reach;       // 1: cells of the cutoff, 27-cell stencil; 2: half cells, 125-cell stencil
   float skin;      // > 0: lists of pairs within 1 + skin kept until a rebuild (reach 1)
+  int lanes;       // pass 2: lanes per particle (8, 16 or 32)
+  int fblk;        // pass 2: 128-row blocks per CTA (1, 2 or 4)
 };
 // Pass 1 and its densities (verlet: over the kept lists; marks: also the
 // precursor marks, zeroed first over rows, the buffer's capacity).
-void launch_density(const DevState& d, int nblk, bool fp64, int reach, bool verlet, bool marks,
+void launch_density(const DevState& d, int nblk, int mode, int reach, bool verlet, bool marks,
                     size_t rows, cudaStream_t st);
 // Precursor conversion after the force pass (marks: the FP32 pass 1 left its
 // marks; else the cells are swept).
 void launch_precursor(const DevState& d, int nblk, bool marks, cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
-void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
+void launch_verlet_build(const DevState& d, int ncell_tot, int nrep, int reach, cudaStream_t st);
 // Pass 2 (kept: pass 1 ran over the kept lists; rows: the capacity of the
 // force sums, which the FP32 pass zeroes first, since its terms arrive by
 // atomic add).
-void launch_force(const DevState& d, int nblk, bool fp64, bool with_press, bool kept,
+void launch_force(const DevState& d, int nblk, int mode, bool with_press, bool kept,
                   const PairTuning& tu, int form_mask, size_t rows, cudaStream_t st);
 void launch_com(const DevState& d, int nblk, double* cm_out, uint32_t* cnt_out, cudaStream_t st);
+// The sum of npair over rows [row0, row0 + n) into *out (device), zeroed first.
+void launch_sum_pairs(const uint32_t* npair, int row0, int n, unsigned long long* out,
+                      cudaStream_t st);
+// The FP64 pass-2 kernels (plain and engine algorithm), launched by launch_force.
+void launch_force_fp64(const DevState& d, int nblk, int mode, bool with_press, bool kept,
+                       cudaStream_t st);
 
 // kernels_chem.cu: one RandomChemEvent (LOCAL_CHEM_EVENT form) on replica 0.
 // force: run regardless of Parameter::time >= beg_chem (fine-grained call).

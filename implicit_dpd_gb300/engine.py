@@ -33,6 +33,7 @@ EXPORTS = [
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
     "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
     "idpd_write_xyz", "idpd_list_rebuilds", "idpd_set_precursor", "idpd_precursor_count",
+    "idpd_pair_count",
 ]
 
 # The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
@@ -88,6 +89,7 @@ def load(path=LIB_PATH):
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_list_rebuilds.argtypes = [H, C.POINTER(C.c_uint64)]
+    L.idpd_pair_count.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64)]
     L.idpd_set_precursor.argtypes = [H, C.c_int32, C.POINTER(IdpdPrecursor)]
     L.idpd_precursor_count.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64)]
     L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
@@ -269,7 +271,9 @@ class Engine:
         nt = min(info.n_targets, max_targets)
         return {"n_targets": info.n_targets, "events": info.events, "stopped": bool(info.stopped),
                 "amp_num": info.amp_num, "targets": t[: 2 * nt].reshape(-1, 2),
-                "core_raw": np.array([list(r) for r in info.core_raw])}
+                "core_raw": np.array([list(r) for r in info.core_raw]),
+                "h2t": np.array([list(r) for r in info.h2t])[: info.n_core],
+                "core_h": np.array([list(r) for r in info.core_h])[: info.n_core]}
 
     def set_observe(self, period, capacity=4096):
         """Observer records every `period` steps (0: off)."""
@@ -322,15 +326,23 @@ class Engine:
                                             C.cast(ptrs, C.c_void_p)), "retrieve_walks")
         return out
 
-    def set_tuning(self, reach, skin=None):
-        """reach 1 or 2; skin > 0 keeps the neighbour lists between rebuilds
-        (None: keep the current skin)."""
-        if skin is None:
-            cur = IdpdTuning()
-            self._ck(self.L.idpd_get_tuning(self.h, C.byref(cur)), "get_tuning")
-            skin = cur.skin
-        self._ck(self.L.idpd_set_tuning(self.h, C.byref(IdpdTuning(reach=reach, skin=skin))),
-                 "set_tuning")
+    def set_tuning(self, reach, skin=None, lanes=None, blocks=None):
+        """reach 1 or 2; skin > 0 keeps the neighbour lists between rebuilds;
+        lanes (8, 16, 32) and blocks (1, 2, 4) shape the force pass (None:
+        keep the current value)."""
+        cur = IdpdTuning()
+        self._ck(self.L.idpd_get_tuning(self.h, C.byref(cur)), "get_tuning")
+        t = IdpdTuning(reach=reach, skin=cur.skin if skin is None else skin,
+                       pair_lanes=cur.pair_lanes if lanes is None else lanes,
+                       pair_blocks=cur.pair_blocks if blocks is None else blocks)
+        self._ck(self.L.idpd_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def tuning(self):
+        """The current tuning as a dict (reach, skin, lanes, blocks)."""
+        t = IdpdTuning()
+        self._ck(self.L.idpd_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return {"reach": t.reach, "skin": round(float(t.skin), 6), "lanes": t.pair_lanes,
+                "blocks": t.pair_blocks}
 
     def set_precursor(self, prop_from, prop_near, prop_to, threshold, seed, replica=0,
                       enabled=True):
@@ -349,6 +361,12 @@ class Engine:
         """Steps that rebuilt the cells and kept lists (0 with skin 0)."""
         n = C.c_uint64()
         self._ck(self.L.idpd_list_rebuilds(self.h, C.byref(n)), "list_rebuilds")
+        return n.value
+
+    def pair_count(self, replica=0):
+        """Ordered pairs within the cutoff (r < 1) of the last density pass."""
+        n = C.c_uint64()
+        self._ck(self.L.idpd_pair_count(self.h, replica, C.byref(n)), "pair_count")
         return n.value
 
     def get_tuning(self):

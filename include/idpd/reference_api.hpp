@@ -14,8 +14,11 @@
 //   ForceBonded<Tpsys>(sys, buf_size, amp_num, core_amp_id), CalcListedForce(sys, vir),
 //   glob_topol(), ExpandTopolBuffer(n)  bdf_calculator.hpp:16-51,90-92,191-220
 //                                                    ForceBonded<Tpsys> (same members)
-//   ChemManager<FP>(seed), RandomChemEvent(sys, glob_topol, param)
-//     chemmanager.hpp:176-180,244-281               ChemManager<FP> (same members)
+//   ChemManager<FP>(seed), RandomChemEvent(sys, glob_topol, param), h2t_vecs(),
+//   core_poss_h()  chemmanager.hpp:176-189,244-281  ChemManager<FP> (same members)
+//   Saru(s1, s2, s3), u32(), uni_open(), nrml()
+//     saruprng.hpp:89,114,123-125,239-255,322-333,427-445
+//                                                    Saru (host, same members)
 //
 // The particle system is duck-typed like FDPS's ParticleSystem<FPDPD>:
 // sys.getNumberOfParticleLocal(), sys[i].{pos, vel, acc, press, delta_sumr}
@@ -36,6 +39,8 @@
 // the engine's message (no exception crosses the C ABI).
 #pragma once
 
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -53,6 +58,53 @@ inline void check(const idpd_handle* h, int rc, const char* what) {
   std::fprintf(stderr, "idpd: %s failed (status %d): %s\n", what, rc, msg);
   std::abort();
 }
+
+// Saru on the host (saruprng.hpp:83-445): the 3-seed constructor, u32(),
+// uni_open() and nrml() with the reference's semantics, for host code that
+// draws from the same counter-based streams as the pair kernels. The integer
+// draws are bit-exact with the reference; uni_open() and nrml() are its FP64
+// expressions (nrml draws its logarithm's argument first, as the reference's
+// build evaluates sqrt(-2 log(uni_open())) * cos(2 pi uni_open())).
+class Saru {
+ public:
+  Saru(uint32_t a, uint32_t b, uint32_t c) {
+    // the seeding hash of saruprng.hpp:239-255
+    c ^= (a << 7) ^ (b >> 6);
+    b += (a >> 4) ^ (c >> 15);
+    a ^= (b << 9) + (c << 8);
+    c ^= 0xA5366B4Du * ((b >> 11) ^ (a << 1));
+    b += 0x72BE1579u * ((a << 4) ^ (c >> 16));
+    a ^= 0x3F38A6EDu * ((c >> 5) ^ sar(b, 22));
+    b += a * c;
+    a += c ^ (b >> 2);
+    b ^= sar(b, 17);
+    lcg_ = 0x79dedea3u * (a ^ sar(a, 14));
+    weyl_ = (lcg_ + b) ^ sar(lcg_, 8);
+    lcg_ = lcg_ + (weyl_ * (weyl_ ^ 0xdddf97f5u));
+    weyl_ = 0xABCB96F7u + (weyl_ >> 1);
+  }
+  // one LCG and Weyl step, then the output mix (saruprng.hpp:173-177,199-202,322-333)
+  uint32_t u32() {
+    lcg_ = 0x4beb5d59u * lcg_ + 0x2600e1f7u;
+    weyl_ = weyl_ + 0x8009d14bu + (sar(weyl_, 31) & 0xda879addu);
+    const uint32_t v = (lcg_ ^ (lcg_ >> 26)) + weyl_;
+    return (v ^ (v >> 20)) * 0x6957f5a7u;
+  }
+  // (0, 1) from 31 bits (saruprng.hpp:427-434)
+  double uni_open() {
+    return ((double)(int32_t)(u32() >> 1) + 0.5) * (1.0 / 2147483648.0);
+  }
+  // Box-Muller normal (saruprng.hpp:442-445)
+  double nrml() {
+    const double u1 = uni_open();
+    const double u2 = uni_open();
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+  }
+
+ private:
+  static uint32_t sar(uint32_t x, int s) { return (uint32_t)((int32_t)x >> s); }
+  uint32_t lcg_, weyl_;
+};
 
 class Session {
  public:
@@ -384,13 +436,31 @@ class ChemManager {
     idpd_chem_info info;
     check(s.handle(), idpd_chem_get_info(s.handle(), 0, &info, nullptr, 0), "idpd_chem_get_info");
     param.amp_num = info.amp_num;
+    h2t_.resize(info.n_core);
+    core_h_.resize(info.n_core);
+    for (int k = 0; k < info.n_core; k++) {
+      h2t_[k] = Vec3{info.h2t[k][0], info.h2t[k][1], info.h2t[k][2]};
+      core_h_[k] = Vec3{info.core_h[k][0], info.core_h[k][1], info.core_h[k][2]};
+    }
     return cont != 0;
   }
+
+  // Per core particle, the unit head-to-tail vector (membrane normal) and the
+  // projected core position of the last event (chemmanager.hpp:123-135,
+  // 183-189), the arrays Observer::MembNormalVect reads (observer.hpp:276);
+  // empty before the first event. The reference declares both arrays but
+  // never fills them.
+  struct Vec3 {
+    double x, y, z;
+  };
+  const std::vector<Vec3>& h2t_vecs() const { return h2t_; }
+  const std::vector<Vec3>& core_poss_h() const { return core_h_; }
 
  private:
   uint32_t seed_;
   int32_t reserve_;
   bool configured_ = false;
+  std::vector<Vec3> h2t_, core_h_;
 };
 
 }  // namespace idpd

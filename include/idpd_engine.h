@@ -107,6 +107,10 @@ typedef struct idpd_config {
 
 #define IDPD_CFG_FP64_PAIRS 0x1 /* plain FP64 pair kernels (baseline arm)       */
 #define IDPD_CFG_TIMING 0x2     /* record per-kernel CUDA events                */
+/* The engine's own algorithm (kept lists, each pair once, 64-bit fixed-point
+ * sums) with FP64 pair arithmetic: the FP32 engine's denominator with the
+ * algorithm held fixed. Cell reach 1 only; excludes IDPD_CFG_FP64_PAIRS. */
+#define IDPD_CFG_FP64_KEPT 0x4
 
 int idpd_create(const idpd_config* cfg, idpd_handle** out);
 int idpd_destroy(idpd_handle* h);
@@ -219,6 +223,14 @@ typedef struct idpd_chem_info {
   /* GetCorePos of the last event per core: core position, hydrophobic and
    * hydrophilic neighbour centres of mass (nei_cm_pos[Hyphob], [Hyphil]) */
   double core_raw[IDPD_CHEM_MAX_CORE][9];
+  /* DetermineTargetIdWithCorePos of the last event per core: the unit
+   * head-to-tail vector (membrane normal) and the projected core position,
+   * what ChemManager::h2t_vecs() / core_poss_h() name (chemmanager.hpp:183-189;
+   * the reference declares both arrays but never fills them) */
+  int32_t n_core;
+  int32_t reserved;
+  double h2t[IDPD_CHEM_MAX_CORE][3];
+  double core_h[IDPD_CHEM_MAX_CORE][3];
 } idpd_chem_info;
 /* State of the last event; targets (may be NULL) receives up to cap pairs of
  * (head, tail) rows of the converted molecules in upload order. */
@@ -365,8 +377,9 @@ int idpd_write_xyz(const char* path, int32_t append, uint32_t time, int32_t n, c
                    const uint32_t* unit);
 
 /* ---- tuning --------------------------------------------------------------- */
-/* Launch and cell-grid shape of the pair passes. Every reach gives the same
- * results bit for bit (all pair sums are fixed point); only speed changes. */
+/* Launch and cell-grid shape of the pair passes. Every reach and launch shape
+ * gives the same results bit for bit (all pair sums are fixed point); only
+ * speed changes. */
 typedef struct idpd_tuning {
   int32_t reach;        /* 1: cells >= rc, 27-cell stencil; 2: cells >= rc/2, 125 cells */
   float skin;           /* > 0: keep each particle's list of pairs within rc + skin and
@@ -375,13 +388,21 @@ typedef struct idpd_tuning {
                            side >= 3 (rc + skin)). Pair sets stay exact; sums differ
                            from skin 0 only by FP32 rounding of the cell-local
                            coordinates. 0: cells and lists every step. */
-  int32_t reserved[6];
+  int32_t pair_lanes;   /* pass 2: lanes per particle, 8, 16 or 32 (0: 16)        */
+  int32_t pair_blocks;  /* pass 2: 128-row blocks per CTA, 1, 2 or 4 (0: 1)        */
+  int32_t reserved[4];
 } idpd_tuning;
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t);
 int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t);
 /* Steps that rebuilt the cells and the kept lists since the lists were last
  * (re)allocated; 0 while the skin is 0. */
 int idpd_list_rebuilds(idpd_handle* h, uint64_t* rebuilds);
+/* Ordered pairs within the cutoff (r < 1, i != j, the pair set of
+ * CalcForceEpEpDPD, nbdf_calculator.hpp:84-88) of replica `replica`, counted
+ * exactly by the last density pass (the last step's, or idpd_density's): the
+ * sum over particles of n_p, the pairs per particle of the pair passes'
+ * roofline. 0 before the first density pass. */
+int idpd_pair_count(idpd_handle* h, int32_t replica, uint64_t* ordered_pairs);
 
 /* ---- timing -------------------------------------------------------------- */
 /* Elapsed milliseconds of the last idpd_step call measured with CUDA events
@@ -403,15 +424,20 @@ int idpd_saru_nrml_f32(int32_t n, const uint32_t* s1, const uint32_t* s2, const 
 
 /* ---- cell list (the FDPS gather replacement) ----------------------------- */
 /* Cell index per particle row and the stable cell-sorted order of the rows
- * for replica `replica` (grid: floor(box/r_cell) cells per axis, r_cell the
- * pair cutoff 1.0). perm[k] = row at sorted position k. */
+ * for replica `replica` on the handle's search grid: floor(box / (1 + skin))
+ * * reach cells per axis (idpd_set_tuning; floor(box) cells of the pair
+ * cutoff 1.0 at the default reach 1, skin 0). perm[k] = row at sorted
+ * position k. */
 int idpd_cell_order(idpd_handle* h, int32_t replica, uint32_t* cell_of_row, uint32_t* perm);
 
 /* ---- cell order without allocation ---------------------------------------
- * No counterpart in the reference. The same cell index per row and stable
- * cell-sorted order as idpd_cell_order, for rows the caller already holds on
- * the device, computed without allocating any device memory. It is meant for
- * callers that cannot call cudaMalloc: a host MD code whose own memory pool
+ * No counterpart in the reference. A cell index per row and the stable
+ * cell-sorted order of the rows, on a grid of floor(box) cells per axis (cells
+ * of the pair cutoff 1.0), for rows the caller already holds on the device,
+ * computed without allocating any device memory. This is idpd_cell_order's
+ * result at the engine's default tuning (cell reach 1, skin 0) only; other
+ * tunings give idpd_cell_order other grids. It is meant for callers that
+ * cannot call cudaMalloc: a host MD code whose own memory pool
  * owns the device budget, or a step loop that must not pay the device-wide
  * synchronisation that cudaMalloc / cudaFree can cause.
  *
@@ -428,9 +454,12 @@ int idpd_cell_order(idpd_handle* h, int32_t replica, uint32_t* cell_of_row, uint
  *   stream       cudaStream_t to queue the work on (NULL: default stream)
  *
  * The call queues its work and returns; the outputs are complete when the
- * stream reaches that point. The first call on each device, made with that
- * device current, looks up the scratch address once: make that first call
- * before any stream capture. All calls share the one array, which keeps the
+ * stream reaches that point. Every call looks the scratch address up in the
+ * context current on the calling thread (cudaGetSymbolAddress, which
+ * allocates nothing), so switching contexts or resetting the device between
+ * calls is safe. The first call on each device also loads the library's
+ * device code there (set-up): make that first call before any stream
+ * capture. All calls share the one array, which keeps the
  * last call's contents, so calls that overlap on the GPU (other streams,
  * other threads) race and corrupt each other's results: serialise them.
  * Errors are read with idpd_last_error(NULL, ...). */

@@ -322,6 +322,39 @@ int orc_density(const idpd_params* p, int32_t n, const double* pos, const uint32
   return 0;
 }
 
+/* Ordered pairs within the cutoff (r < 1, i != j): the pair set of
+ * CalcForceEpEpDPD (nbdf_calculator.hpp:84-88) counted over the image-shifted
+ * cells, for the pairs-per-particle figure of the CPU baseline. */
+int64_t orc_pair_count(const idpd_params* p, int32_t n, const double* pos, int32_t nthreads) {
+  orc_grid g;
+  if (grid_build(&g, n, pos, p->box) != 0) return -1;
+  int64_t total = 0;
+  (void)nthreads;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : total) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int32_t c = 0; c < g.ncell; c++) {
+    const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    for (int32_t m = g.start[c]; m < g.start[c + 1]; m++) {
+      const int32_t i = g.members[m];
+      for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            double sh[3];
+            const int32_t cj = nbr_cell(&g, p->box, cx, cy, cz, dx, dy, dz, sh);
+            for (int32_t mj = g.start[cj]; mj < g.start[cj + 1]; mj++) {
+              const int32_t j = g.members[mj];
+              if (j == i) continue;
+              const double ddx = pos[3 * i] - (pos[3 * j] + sh[0]),
+                           ddy = pos[3 * i + 1] - (pos[3 * j + 1] + sh[1]),
+                           ddz = pos[3 * i + 2] - (pos[3 * j + 2] + sh[2]);
+              total += (ddx * ddx + ddy * ddy + ddz * ddz) < 1.0;
+            }
+          }
+    }
+  }
+  grid_free(&g);
+  return total;
+}
+
 /* ------------------------------------------------- precursor conversion */
 /* Saru 3-seed constructor and u32 (saruprng.hpp:239-255, 322-333) keyed on
  * (id, time, seed); the pair test of pass 1 (nbdf_calculator.hpp:27-29). */

@@ -105,6 +105,7 @@ int64_t orc_precursor(const idpd_params* p, int32_t n, const double* pos, const 
                       uint32_t* prop, uint32_t time, uint32_t from, uint32_t near, uint32_t to,
                       uint32_t threshold, uint32_t seed, int32_t nthreads);
 
+int64_t orc_pair_count(const idpd_params* p, int32_t n, const double* pos, int32_t nthreads);
 int64_t orc_pairs_naive(int32_t n, const double* pos, const double* box, double rc,
                         uint32_t* pi, uint32_t* pj, int64_t cap);
 

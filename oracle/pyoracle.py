@@ -14,6 +14,9 @@ from implicit_dpd_gb300.abi import IdpdChemParams, IdpdParams, IdpdRunParam
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libidpd_oracle.so")
+# the same restatement built with the reference's production flags
+# (-O3 -ffast-math -funroll-loops, Makefile:10,21-23): CPU timing only
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libidpd_oracle_fast.so")
 
 _lib = None
 
@@ -33,41 +36,55 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
-        L = C.CDLL(LIB_PATH)
-        L.orc_saru_u32.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, U]
-        L.orc_saru_nrml.restype = C.c_double
-        L.orc_saru_nrml.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
-        L.orc_mt_draws.argtypes = [C.c_uint32, C.c_int32, U]
-        L.orc_mt_seed.argtypes = [C.POINTER(OrcMT), C.c_uint32]
-        L.orc_derive_params.argtypes = [C.POINTER(IdpdRunParam), C.POINTER(IdpdParams)]
-        L.orc_cells.restype = C.c_int32
-        L.orc_cells.argtypes = [C.c_int32, D, D, C.c_double, I, I, I, I]
-        L.orc_density.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, U, D, C.c_void_p,
-                                  C.c_void_p, C.c_int32]
-        L.orc_force.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, U, U, D, D, C.c_void_p,
-                                C.c_int32]
-        L.orc_build_topology.argtypes = [C.c_int32, U, U, C.c_int32, C.c_int32, U, C.c_double,
-                                         C.c_double, U, D]
-        L.orc_bonded.argtypes = [C.POINTER(IdpdParams), C.c_int32, U, D, D, D, D]
-        L.orc_drift.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, C.c_void_p, D, C.c_void_p]
-        L.orc_kick.argtypes = [C.c_double, C.c_int32, D, D, D]
-        L.orc_remove_cmdrift.argtypes = [C.c_int32, D]
-        L.orc_md_step.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, D, D, D, U, U, C.c_int32,
-                                  C.c_void_p, C.c_void_p, D, D, D, C.c_int32]
-        L.orc_chem_event.argtypes = [C.POINTER(IdpdParams), C.POINTER(IdpdChemParams),
-                                     C.POINTER(OrcMT), C.POINTER(C.c_int32), C.c_int32, D, D, D, D,
-                                     D, U, U, U, U, D, U, C.c_int32, U, C.POINTER(C.c_uint32),
-                                     C.c_void_p, C.POINTER(C.c_int32)]
-        L.orc_precursor.restype = C.c_int64
-        L.orc_precursor.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, U, U, C.c_uint32,
-                                    C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
-                                    C.c_int32]
-        L.orc_pairs_naive.restype = C.c_int64
-        L.orc_pairs_naive.argtypes = [C.c_int32, D, D, C.c_double, U, U, C.c_int64]
-        _lib = L
+        _lib = _load(LIB_PATH)
     return _lib
+
+
+def use_fast_build(on):
+    """Routes every wrapper below to the build with the reference's
+    production flags (on) or back to the parity build (off). Timing only: the
+    fast-math build is not a parity oracle."""
+    global _lib
+    _lib = _load(FAST_LIB_PATH if on else LIB_PATH)
+
+
+def _load(path):
+    if not os.path.exists(path):
+        build()
+    L = C.CDLL(path)
+    L.orc_saru_u32.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, U]
+    L.orc_saru_nrml.restype = C.c_double
+    L.orc_saru_nrml.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+    L.orc_mt_draws.argtypes = [C.c_uint32, C.c_int32, U]
+    L.orc_mt_seed.argtypes = [C.POINTER(OrcMT), C.c_uint32]
+    L.orc_derive_params.argtypes = [C.POINTER(IdpdRunParam), C.POINTER(IdpdParams)]
+    L.orc_cells.restype = C.c_int32
+    L.orc_cells.argtypes = [C.c_int32, D, D, C.c_double, I, I, I, I]
+    L.orc_density.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, U, D, C.c_void_p,
+                              C.c_void_p, C.c_int32]
+    L.orc_force.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, U, U, D, D, C.c_void_p,
+                            C.c_int32]
+    L.orc_build_topology.argtypes = [C.c_int32, U, U, C.c_int32, C.c_int32, U, C.c_double,
+                                     C.c_double, U, D]
+    L.orc_bonded.argtypes = [C.POINTER(IdpdParams), C.c_int32, U, D, D, D, D]
+    L.orc_drift.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, C.c_void_p, D, C.c_void_p]
+    L.orc_kick.argtypes = [C.c_double, C.c_int32, D, D, D]
+    L.orc_remove_cmdrift.argtypes = [C.c_int32, D]
+    L.orc_md_step.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, D, D, D, D, U, U, C.c_int32,
+                              C.c_void_p, C.c_void_p, D, D, D, C.c_int32]
+    L.orc_chem_event.argtypes = [C.POINTER(IdpdParams), C.POINTER(IdpdChemParams),
+                                 C.POINTER(OrcMT), C.POINTER(C.c_int32), C.c_int32, D, D, D, D,
+                                 D, U, U, U, U, D, U, C.c_int32, U, C.POINTER(C.c_uint32),
+                                 C.c_void_p, C.POINTER(C.c_int32)]
+    L.orc_precursor.restype = C.c_int64
+    L.orc_precursor.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, U, U, C.c_uint32,
+                                C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                C.c_int32]
+    L.orc_pairs_naive.restype = C.c_int64
+    L.orc_pairs_naive.argtypes = [C.c_int32, D, D, C.c_double, U, U, C.c_int64]
+    L.orc_pair_count.restype = C.c_int64
+    L.orc_pair_count.argtypes = [C.POINTER(IdpdParams), C.c_int32, D, C.c_int32]
+    return L
 
 
 def _ptr(a):
@@ -241,6 +258,14 @@ def precursor(p, pos, pid, prop, time, from_, near, to, threshold, seed, nthread
     if cnt < 0:
         raise ValueError("box too small for the cell grid")
     return out, int(cnt)
+
+
+def pair_count(p, pos, nthreads=1):
+    """Ordered pairs within the cutoff (r < 1, i != j)."""
+    c = lib().orc_pair_count(C.byref(p), len(pos), np.ascontiguousarray(pos, np.float64), nthreads)
+    if c < 0:
+        raise ValueError("box too small for the cell grid")
+    return int(c)
 
 
 def pairs_naive(pos, box, rc=1.0):

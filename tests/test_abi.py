@@ -129,3 +129,21 @@ def test_cpp_adapters_compile_and_link(lib, tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     assert os.path.exists(exe)
+
+
+def test_host_saru_adapter_matches_reference_golden(tmp_path):
+    """The host Saru of the C++ adapters against the golden draws of the
+    reference's saruprng.hpp: u32() bit-exact, nrml() to FP64 rounding (the
+    host libm's log and cos)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "saru.npz"))
+    exe = os.path.join(str(tmp_path), "saru_host")
+    subprocess.run(["g++", "-O2", "-std=c++11", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "saru_host.cpp"), "-o", exe], check=True)
+    seeds = g["seeds"]
+    inp = "\n".join(f"{a} {b} {c}" for a, b, c in seeds) + "\n"
+    out = subprocess.run([exe], input=inp, capture_output=True, text=True, check=True).stdout
+    rows = [line.split() for line in out.strip().splitlines()]
+    u = np.array([[int(x) for x in r[:4]] for r in rows], np.uint64).astype(np.uint32)
+    nr = np.array([float(r[4]) for r in rows])
+    assert np.array_equal(u, g["u32"][:, :4])
+    assert np.abs(nr - g["nrml"]).max() < 1e-14 * max(1.0, np.abs(g["nrml"]).max())

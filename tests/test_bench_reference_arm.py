@@ -28,5 +28,8 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    # the sample's pair density and the host it ran on are part of the record
+    assert 50 < cb["pairs_per_bead"] < 400
+    assert cb["nproc"] >= 1 and "cpu_model" in cb and "omp_num_threads" in cb
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}

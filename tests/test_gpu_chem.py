@@ -76,6 +76,22 @@ def test_core_geometry_matches_oracle_density():
         assert np.abs(info["core_raw"][k][6:9] - cm[row, :3]).max() < FP_TOL
         assert np.abs(info["core_raw"][k][3:6] - cm[row, 3:]).max() < FP_TOL
     assert info["n_targets"] == 0 and info["events"] == 1
+    # h2t_vecs() / core_poss_h(): the unit head-to-tail vector and the
+    # projected core position of DetermineTargetIdWithCorePos
+    # (chemmanager.hpp:123-135) from the same core geometry
+    box = np.asarray(BOX, np.float64)
+    assert len(info["h2t"]) == len(core_ptcl) == len(info["core_h"])
+    for k in range(len(core_ptcl)):
+        raw = info["core_raw"][k]
+        h2t = raw[3:6] - raw[:3]
+        h2t -= box * np.round(h2t / box)
+        h2t /= np.sqrt((h2t * h2t).sum())
+        c2cm = raw[6:9] - raw[:3]
+        c2cm -= box * np.round(c2cm / box)
+        core_h = raw[:3] + (c2cm @ h2t) * h2t
+        core_h -= np.floor(core_h / box) * box
+        assert np.abs(info["h2t"][k] - h2t).max() < 1e-12
+        assert np.abs(info["core_h"][k] - core_h).max() < 1e-12
 
 
 def test_chem_event_decisions_bit_exact_two_events():

@@ -188,3 +188,28 @@ def test_pair_set_matches_naive_minimum_image():
                         for j in js[(r2 < 1.0) & (js != i)]:
                             got.add((int(i), int(j)))
     assert got == naive
+
+
+def test_pair_count_and_production_flag_build():
+    """The oracle's pair count equals the naive count of pairs within the
+    cutoff; the build with the reference's production flags (-O3 -ffast-math
+    -funroll-loops, timed as the second CPU figure) computes the same pass-2
+    forces to FP64 rounding."""
+    from implicit_dpd_gb300 import configs
+
+    box = np.array([6.0, 7.0, 6.5])
+    st = configs.liquid(box, 4.0, seed=3)
+    rp = configs.run_param(box)
+    p = O.derive_params(rp)
+    p.seed, p.time = 5, 2
+    pi, pj = O.pairs_naive(st["pos"], box, 1.0)
+    assert O.pair_count(p, st["pos"], 2) == len(pi)
+    dens, _, _ = O.density(p, st["pos"], st["prop"])
+    acc, _ = O.force(p, st["pos"], st["vel"], st["id"], st["prop"], dens)
+    O.use_fast_build(True)
+    try:
+        dens_f, _, _ = O.density(p, st["pos"], st["prop"])
+        acc_f, _ = O.force(p, st["pos"], st["vel"], st["id"], st["prop"], dens_f)
+    finally:
+        O.use_fast_build(False)
+    assert np.abs(acc_f - acc).max() < 1e-9 * np.abs(acc).max()

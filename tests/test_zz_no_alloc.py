@@ -5,9 +5,10 @@ owns the whole device budget, or a step loop that must not pay the
 device-wide synchronisation of cudaMalloc / cudaFree. This entry point serves
 them from one static scratch array of the library. These tests hand it
 device buffers owned by the caller (torch here) and check its output against
-the engine's own idpd_cell_order, which is integer work and must agree bit
-for bit, on two calls in a row (the second call must not see the first
-call's counts). The file runs last so that a run stopping at the first
+the engine's own idpd_cell_order at its default tuning (cell reach 1, skin
+0), which is integer work and must agree bit for bit: two calls in a row on
+the same buffers, then the same on a smaller grid (the scratch keeps the
+larger grid's counts, which the next call must not see). The file runs last so that a run stopping at the first
 failure has already run every other test.
 """
 import ctypes as C
@@ -47,9 +48,10 @@ def _engine_order(box, st):
 
 
 def _systems():
+    """The larger grid first (13 x 12 x 14 cells), then a smaller one (9 x 10 x 11)."""
     box1, st1, _ = mixed_system()
     st2 = configs.liquid((13.5, 12.0, 14.7), 3.0, seed=5)
-    return [(np.asarray(box1, np.float64), st1), (np.array([13.5, 12.0, 14.7]), st2)]
+    return [(np.array([13.5, 12.0, 14.7]), st2), (np.asarray(box1, np.float64), st1)]
 
 
 def test_noalloc_cell_order_matches_cell_order_on_two_calls():
@@ -59,13 +61,39 @@ def test_noalloc_cell_order_matches_cell_order_on_two_calls():
         pos_d = torch.from_numpy(st["pos"]).to("cuda")
         cell_d = torch.full((n,), -1, dtype=torch.int32, device="cuda")
         perm_d = torch.full((n,), -1, dtype=torch.int32, device="cuda")
-        rc = _noalloc(pos_d, n, box, cell_d, perm_d)
-        assert rc == IDPD_OK, last_error()
-        torch.cuda.synchronize()
-        cell = cell_d.cpu().numpy().view(np.uint32)
-        perm = perm_d.cpu().numpy().view(np.uint32)
-        assert np.array_equal(cell, cell_ref)
-        assert np.array_equal(perm, perm_ref)
+        for call in range(2):  # two calls in a row on the same buffers
+            rc = _noalloc(pos_d, n, box, cell_d, perm_d)
+            assert rc == IDPD_OK, last_error()
+            torch.cuda.synchronize()
+            cell = cell_d.cpu().numpy().view(np.uint32)
+            perm = perm_d.cpu().numpy().view(np.uint32)
+            assert np.array_equal(cell, cell_ref), f"call {call}"
+            assert np.array_equal(perm, perm_ref), f"call {call}"
+
+
+def test_noalloc_grid_is_the_default_tuning_grid_only():
+    # reach 2 gives idpd_cell_order twice the cells per axis; the
+    # allocation-free call keeps floor(box) cells per axis
+    box = np.array([13.5, 12.0, 14.7])
+    st = configs.liquid(box, 3.0, seed=5)
+    n = len(st["pos"])
+    e = Engine()
+    e.set_params(mdpd_params(box))
+    e.upload(st)
+    e.set_tuning(2, 0.0)
+    cell2, _ = e.cell_order()
+    e.close()
+    pos_d = torch.from_numpy(st["pos"]).to("cuda")
+    cell_d = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    perm_d = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    assert _noalloc(pos_d, n, box, cell_d, perm_d) == IDPD_OK, last_error()
+    torch.cuda.synchronize()
+    cell1 = cell_d.cpu().numpy().view(np.uint32)
+    nc1 = np.floor(box).astype(np.int64)
+    inv_cs = nc1 / box  # cell index = trunc(x * (nc / box)), clamped to the grid
+    c1 = np.clip((st["pos"] * inv_cs).astype(np.int64), 0, nc1 - 1)
+    assert np.array_equal(cell1, (c1[:, 2] * nc1[1] + c1[:, 1]) * nc1[0] + c1[:, 0])
+    assert cell2.max() >= np.prod(nc1)  # the reach-2 grid has 8x the cells
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
