@@ -149,15 +149,24 @@ class Clocks:
         self.path = None
 
     def start(self):
+        """Starts sampling every 20 ms and returns once the first sample is
+        written (nvidia-smi takes ~0.1 s to start), so that even a timed region
+        of a few tens of ms falls inside the sampled window."""
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.005)
 
     def stop(self):
         if self.proc is None:
@@ -234,21 +243,6 @@ def profiled_traffic(name):
             except ValueError:
                 return None
     return None
-
-
-def profiled_inst_per_bead(name):
-    """Warp instructions per bead of a kernel from its committed ncu summary
-    (smsp__inst_executed.sum of the captured launch over its beads)."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    inst, beads = None, None
-    for line in open(path):
-        if "`smsp__inst_executed.sum`" in line:
-            inst = float(line.split("|")[2].split()[0])
-        if line.startswith("DRAM traffic of the captured launch:"):
-            beads = float(line.split(" for ")[1].split()[0])
-    return inst / beads if inst and beads else None
 
 
 def equilibrated_patch(threads, equil=2000):
@@ -403,7 +397,7 @@ def reaction_bench(tune, steps=100, equil=2000, device=0):
     n = len(both["pos"])
     both["id"] = np.arange(n, dtype=np.uint32)
     e = make_engine(both, n_amp, rp, device=device)
-    e.set_tuning(tune["reach"], tune["skin"])
+    e.set_tuning(tune["reach"], tune["skin"], lanes=tune.get("lanes"), blocks=tune.get("blocks"))
     e.step(equil)
     e.set_precursor(SOLVENT, HYPHOB, HYPHIL, precursor_threshold(1e-4), 2024)
     e.step(3)
@@ -572,7 +566,13 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     eb.step(3)
     dist.barrier()
     eb.step(steps)
+    graph_ms = eb.last_step_ms() / steps
     batched = n_tot * steps / (dist.max(eb.last_step_ms()) * 1e-3)
+    # what one persistent launch could save at most: the graph step's time
+    # beyond its kernels' own times (CUDA events of un-graphed profile steps,
+    # median of 5; the events add their own gaps, so this bounds from above)
+    prof = [eb.profile_step() for _ in range(5)]
+    kernels_ms = sum(statistics.median(p_[k] for p_ in prof) for k in prof[0])
     eb.close()
     singles = []
     for i in mine:
@@ -596,6 +596,8 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
             "steps": steps, "tuning": {"reach": reach, "skin": skin},
             "batched": batched, "one_at_a_time": one_at_a_time,
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
+            "graph_ms_per_step": graph_ms, "kernels_ms_per_step": kernels_ms,
+            "launch_gap_share": max(0.0, graph_ms - kernels_ms) / graph_ms,
             "partition": {"ranks": world, "rule": "greedy LPT on particle counts",
                           "replicas_per_rank": [len(p) for p in parts],
                           "particles_per_rank": loads, "imbalance": imbalance(loads)},
@@ -649,9 +651,10 @@ def pinned(shape):
 
 
 def autotune(e, steps=40):
-    """Times each (cell reach, skin) on the current state over enough steps
-    to include list rebuilds, and keeps the fastest (the package's tuner,
-    without its cache: the bench measures afresh)."""
+    """Times each (cell reach, skin), then each force-pass shape (lanes per
+    particle, row blocks per CTA), on the current state over enough steps to
+    include list rebuilds, and keeps the fastest (the package's tuner, without
+    its cache: the bench measures afresh)."""
     from implicit_dpd_gb300.autotune import tune
 
     return tune(e, steps=steps)
@@ -751,8 +754,8 @@ def run_engine(args, rank, world, local_rank):
     e.step(args.equil)
     t_eq = time.perf_counter() - t_eq
     if args.reach:
-        e.set_tuning(args.reach, args.skin)
-        reach, tune_ms = {"reach": args.reach, "skin": args.skin}, None
+        e.set_tuning(args.reach, args.skin, lanes=args.lanes, blocks=args.blocks)
+        reach, tune_ms = e.tuning(), None
     else:
         reach, tune_ms = autotune(e)
     if args.save_state and rank == 0:
@@ -861,6 +864,10 @@ def main():
                     help="cell reach (1 or 2) instead of the autotuned one")
     ap.add_argument("--skin", type=float, default=0.0,
                     help="neighbour-list skin with --reach (0: lists every step)")
+    ap.add_argument("--lanes", type=int, default=16,
+                    help="force pass: lanes per particle with --reach (8, 16 or 32)")
+    ap.add_argument("--blocks", type=int, default=1,
+                    help="force pass: 128-row blocks per CTA with --reach (1, 2 or 4)")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     if args.kernel_case:

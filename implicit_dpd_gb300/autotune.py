@@ -1,11 +1,12 @@
 """The engine's autotuner: picks the cell reach and the neighbour-list skin of
-a handle by timing each choice on the handle's current state, and caches the
-choice per GPU model and workload signature in a JSON file.
+a handle, then the launch shape of the force pass (lanes per particle and
+128-row blocks per CTA), by timing each choice on the handle's current state,
+and caches the choice per GPU model and workload signature in a JSON file.
 
-Neither choice changes the pair sets (they are exact), and the fixed-point
-sums make the reach irrelevant to the results; a skin changes them only by
-the FP32 rounding of cell-local coordinates. So tuning is safe to run on the
-production state itself: the steps it times are ordinary steps.
+No choice changes the pair sets (they are exact), and the fixed-point sums
+make the reach and the launch shape irrelevant to the results; a skin changes
+them only by the FP32 rounding of cell-local coordinates. So tuning is safe
+to run on the production state itself: the steps it times are ordinary steps.
 """
 import json
 import math
@@ -13,6 +14,8 @@ import os
 
 DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
                    (2, 0.3))
+# (lanes per particle, row blocks per CTA) of the force pass; the first is the default
+SHAPES = ((16, 1), (8, 1), (32, 1), (8, 2), (16, 2))
 
 
 def default_cache_path():
@@ -49,31 +52,50 @@ def _store(path, table):
     os.replace(tmp, path)
 
 
-def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, refresh=False):
-    """Applies the fastest (reach, skin) to `engine` and returns
-    (choice, times): times maps "reach{r}_skin{s}" to ms per step (empty when
-    the choice came from the cache). With a key and a cache path, a cached
-    choice is applied without timing unless refresh is set, and a new choice
-    is written back. Choices whose skin the box does not allow are skipped."""
+def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, refresh=False,
+         shapes=SHAPES):
+    """Applies the fastest (reach, skin), then the fastest force-pass shape
+    (lanes, blocks) at that (reach, skin), to `engine` and returns (choice,
+    times): choice = {"reach", "skin", "lanes", "blocks"}, times maps
+    "reach{r}_skin{s}" and "lanes{l}_blocks{b}" to ms per step (empty when the
+    choice came from the cache). With a key and a cache path, a cached choice
+    is applied without timing unless refresh is set, and a new choice is
+    written back. Choices whose skin the box does not allow are skipped."""
     table = _load(cache_path) if (cache_path and key) else {}
     if key and not refresh and key in table:
-        reach, skin = table[key]["reach"], table[key]["skin"]
-        engine.set_tuning(reach, skin)
-        return {"reach": reach, "skin": skin}, {}
+        c = table[key]
+        choice = {"reach": c["reach"], "skin": c["skin"], "lanes": c.get("lanes", shapes[0][0]),
+                  "blocks": c.get("blocks", shapes[0][1])}
+        engine.set_tuning(choice["reach"], choice["skin"], lanes=choice["lanes"],
+                          blocks=choice["blocks"])
+        return choice, {}
+
+    def timed():
+        engine.step(2)
+        engine.step(steps)
+        return engine.last_step_ms() / steps
+
+    lanes0, blocks0 = shapes[0]
     times = {}
     for reach, skin in choices:
         try:
-            engine.set_tuning(reach, skin)
+            engine.set_tuning(reach, skin, lanes=lanes0, blocks=blocks0)
         except Exception:  # the box is too small for this skin
             continue
-        engine.step(2)
-        engine.step(steps)
-        times[(reach, skin)] = engine.last_step_ms() / steps
+        times[(reach, skin)] = timed()
     if not times:
         raise ValueError("no tuning choice fits this system")
     reach, skin = min(times, key=times.get)
-    engine.set_tuning(reach, skin)
+    shape_times = {shapes[0]: times[(reach, skin)]}
+    for lanes, blocks in shapes[1:]:
+        engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+        shape_times[(lanes, blocks)] = timed()
+    lanes, blocks = min(shape_times, key=shape_times.get)
+    engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+    choice = {"reach": reach, "skin": skin, "lanes": lanes, "blocks": blocks}
     if cache_path and key:
-        table[key] = {"reach": reach, "skin": skin, "ms_per_step": times[(reach, skin)]}
+        table[key] = dict(choice, ms_per_step=shape_times[(lanes, blocks)])
         _store(cache_path, table)
-    return {"reach": reach, "skin": skin}, {f"reach{r}_skin{s:g}": t for (r, s), t in times.items()}
+    out = {f"reach{r}_skin{s:g}": t for (r, s), t in times.items()}
+    out.update({f"lanes{l}_blocks{b}": t for (l, b), t in shape_times.items()})
+    return choice, out

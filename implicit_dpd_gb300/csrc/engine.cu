@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "idpd_engine.h"
@@ -92,6 +93,16 @@ struct idpd_handle {
   cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
   WalkState* walks = nullptr;           // FDPS multi-walk buffers (created on first use)
   unsigned long long* pair_sum = nullptr;  // device word of idpd_pair_count
+  // asynchronous trajectory frames (idpd_dump_xyz_async): device staging in
+  // upload order, its pinned host copy, the copy stream and the writer thread
+  cudaStream_t dump_st = nullptr;
+  cudaEvent_t dump_ready = nullptr, dump_done = nullptr;
+  unsigned char* dump_dev = nullptr;
+  unsigned char* dump_host = nullptr;
+  size_t dump_cap = 0;
+  std::thread dump_thread;
+  int dump_rc = IDPD_OK;        // first failed frame's status (read by idpd_dump_wait)
+  std::string dump_msg;
   bool pairs_valid = false;             // a density pass has run on the current layout
 };
 
@@ -685,7 +696,7 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_bin_gated(d, h->nblk, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
-    launch_verlet_build(d, h->ncell_tot, h->R, h->tune.reach, h->st);
+    launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   } else {
     launch_drift_bin(d, h->nblk, true, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st);
@@ -857,7 +868,13 @@ int idpd_create(const idpd_config* cfg, idpd_handle** out) {
 int idpd_destroy(idpd_handle* h) {
   if (!h) return IDPD_OK;
   cudaSetDevice(h->device);
+  if (h->dump_thread.joinable()) h->dump_thread.join();
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->dump_dev) cudaFree(h->dump_dev);
+  if (h->dump_host) cudaFreeHost(h->dump_host);
+  if (h->dump_ready) cudaEventDestroy(h->dump_ready);
+  if (h->dump_done) cudaEventDestroy(h->dump_done);
+  if (h->dump_st) cudaStreamDestroy(h->dump_st);
   free_all(h);
   if (h->chem) cudaFree(h->chem);
   if (h->walks) walk_destroy(h->walks);
@@ -1385,6 +1402,91 @@ int idpd_list_rebuilds(idpd_handle* h, uint64_t* rebuilds) {
   return check_device_error(h);
 }
 
+int idpd_dump_xyz_async(idpd_handle* h, int32_t replica, const char* path, int32_t append) {
+  if (!h || !path || replica < 0 || replica >= h->R)
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  cudaSetDevice(h->device);
+  int rc = commit(h);
+  if (rc) return rc;
+  // one frame in flight: the previous one is on disk before its buffers are reused
+  if (h->dump_thread.joinable()) h->dump_thread.join();
+  const RepDev& R = h->reps_h[replica];
+  const int n = R.n;
+  const size_t bytes = 16 + (size_t)n * (9 * sizeof(double) + 4 * sizeof(uint32_t));
+  if (!h->dump_st) {
+    CK(cudaStreamCreateWithFlags(&h->dump_st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->dump_ready, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->dump_done, cudaEventDisableTiming));
+  }
+  if (bytes > h->dump_cap) {
+    if (h->dump_dev) cudaFree(h->dump_dev);
+    if (h->dump_host) cudaFreeHost(h->dump_host);
+    h->dump_dev = nullptr;
+    h->dump_host = nullptr;
+    h->dump_cap = 0;
+    if (cudaMalloc(&h->dump_dev, bytes) != cudaSuccess ||
+        cudaMallocHost(&h->dump_host, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, IDPD_ERR_CAPACITY, "trajectory frame buffers (%zu bytes)", bytes);
+    }
+    h->dump_cap = bytes;
+  }
+  // staging layout: time (u32, padded to 16 bytes), pos, vel, acc (n x 3 doubles
+  // each), id, prop, amp_id, unit (n u32 each), all in upload order
+  const DevState& d = h->d;
+  double* f64 = reinterpret_cast<double*>(h->dump_dev + 16);
+  uint32_t* u32 = reinterpret_cast<uint32_t*>(h->dump_dev + 16 + 9 * sizeof(double) * (size_t)n);
+  CK(cudaMemcpyAsync(h->dump_dev, d.rep_time + replica, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                     h->st));
+  launch_soa_to_aos(d.px, d.py, d.pz, d.loc, R.row_off, f64, n, h->st);
+  launch_soa_to_aos(d.vx, d.vy, d.vz, d.loc, R.row_off, f64 + 3 * (size_t)n, n, h->st);
+  launch_soa_to_aos(d.ax, d.ay, d.az, d.loc, R.row_off, f64 + 6 * (size_t)n, n, h->st);
+  launch_gather_u32x4(d.id, d.prop, d.amp_id, d.unit, d.loc, R.row_off, u32, n, h->st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->dump_ready, h->st));
+  CK(cudaStreamWaitEvent(h->dump_st, h->dump_ready, 0));
+  CK(cudaMemcpyAsync(h->dump_host, h->dump_dev, bytes, cudaMemcpyDeviceToHost, h->dump_st));
+  CK(cudaEventRecord(h->dump_done, h->dump_st));
+  const std::string file(path);
+  const int dev = h->device;
+  h->dump_thread = std::thread([h, file, append, n, dev]() {
+    cudaSetDevice(dev);
+    int frc = IDPD_OK;
+    std::string msg;
+    if (cudaEventSynchronize(h->dump_done) != cudaSuccess) {
+      frc = IDPD_ERR_CUDA;
+      msg = std::string("trajectory frame copy: ") + cudaGetErrorString(cudaGetLastError());
+    } else {
+      const unsigned char* b = h->dump_host;
+      uint32_t t;
+      std::memcpy(&t, b, sizeof(t));
+      const double* f = reinterpret_cast<const double*>(b + 16);
+      const uint32_t* u = reinterpret_cast<const uint32_t*>(b + 16 + 9 * sizeof(double) * (size_t)n);
+      frc = idpd_write_xyz(file.c_str(), append, t, n, f, f + 3 * (size_t)n, nullptr,
+                           f + 6 * (size_t)n, u, u + n, u + 2 * (size_t)n, u + 3 * (size_t)n);
+      if (frc != IDPD_OK) {
+        char m[512];
+        idpd_last_error(nullptr, m, sizeof(m));
+        msg = m;
+      }
+    }
+    if (frc != IDPD_OK && h->dump_rc == IDPD_OK) {
+      h->dump_rc = frc;
+      h->dump_msg = msg;
+    }
+  });
+  return IDPD_OK;
+}
+
+int idpd_dump_wait(idpd_handle* h) {
+  if (!h) return IDPD_ERR_INVALID_ARG;
+  if (h->dump_thread.joinable()) h->dump_thread.join();
+  const int rc = h->dump_rc;
+  h->dump_rc = IDPD_OK;
+  if (rc != IDPD_OK) return fail(h, rc, "trajectory frame: %s", h->dump_msg.c_str());
+  return IDPD_OK;
+}
+
 int idpd_pair_count(idpd_handle* h, int32_t replica, uint64_t* ordered_pairs) {
   if (!h || !ordered_pairs) return fail(h, IDPD_ERR_INVALID_ARG, "null pointer");
   if (replica < 0 || replica >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "replica %d out of range", replica);
@@ -1436,7 +1538,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   CK(cudaEventRecord(ev[2], h->st));
   launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
   CK(cudaEventRecord(ev[3], h->st));
-  if (verlet) launch_verlet_build(d, h->ncell_tot, h->R, h->tune.reach, h->st);
+  if (verlet) launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
   h->pairs_valid = true;
   launch_density(d, h->nblk, mode, h->tune.reach, verlet, false, h->cap, h->st);

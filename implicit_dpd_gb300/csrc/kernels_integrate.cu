@@ -406,6 +406,27 @@ void launch_soa_to_aos(const double* x, const double* y, const double* z, const 
   k_soa_to_aos<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, loc, row0, aos, n);
 }
 
+// The four u32 fields of rows row0 .. row0 + n - 1 in upload order (loc maps
+// upload rows to storage rows): out[f * n + k] = field f of upload row k.
+__global__ void k_gather_u32x4(const uint32_t* a, const uint32_t* b, const uint32_t* c,
+                               const uint32_t* e, const uint32_t* loc, int row0, uint32_t* out,
+                               int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = loc[row0 + k];
+  out[k] = a[i];
+  out[(size_t)n + k] = b[i];
+  out[2 * (size_t)n + k] = c[i];
+  out[3 * (size_t)n + k] = e[i];
+}
+
+void launch_gather_u32x4(const uint32_t* a, const uint32_t* b, const uint32_t* c,
+                         const uint32_t* e, const uint32_t* loc, int row0, uint32_t* out, int n,
+                         cudaStream_t st) {
+  if (n == 0) return;
+  k_gather_u32x4<<<(n + 255) / 256, 256, 0, st>>>(a, b, c, e, loc, row0, out, n);
+}
+
 // ------------------------------------------------------------ observables
 // Observer::KineticTempera, Pressure and Diffusion (observer.hpp:82-178) of
 // the replicas whose step counter is a multiple of the period. Row sums are

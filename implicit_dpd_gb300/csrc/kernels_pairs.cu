@@ -268,41 +268,34 @@ __global__ void __launch_bounds__(kRowBlock) k_dens_finalize(DevState d) {
 // list only has to hold every pair that can come within the cutoff before
 // the next rebuild). Only the candidates the particle owns are kept (owns()
 // on the cell-local x of the build, kept in okey): the stencil's -x third is
-// never queued. A persistent grid (one wave of CTAs) strides over the cells
-// of all replicas, warp w taking cells w, w + W, ...: every warp gets tens of
-// cells of mixed occupancy, so the warps of a CTA finish together. Also
-// records each row's delta_sumr for the displacement test.
-__device__ __forceinline__ int replica_of_cell(const DevState& d, int cell, int nrep) {
-  int lo = 0, hi = nrep - 1;  // the last replica whose first cell is <= cell
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (d.reps[mid].cell_off <= cell) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
+// never queued. Each warp builds the lists of exactly its 32-row chunk, one
+// cell's share of the chunk at a time (a cell split between chunks has its
+// stencil set up by each), so the warps of a CTA carry equal numbers of
+// particles. Also records each row's delta_sumr for the displacement test.
 template <int REACH>
-__global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d, int ncell_tot, int nrep) {
+__global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d) {
   __shared__ SegTable seg[kWarps];
   __shared__ float4 bpos[kWarps][32];
   __shared__ float4 qpos[kWarps][64];
   __shared__ uint32_t qent[kWarps][64];
   if (!d.vdev->rebuild) return;
+  const int r = d.blk_rep[blockIdx.x];
+  const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SegTable& S = seg[wid];
   float4* P = bpos[wid];
   float4* QX = qpos[wid];
   uint32_t* QE = qent[wid];
   const uint32_t lt_mask = (1u << lane) - 1u;
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
   const float rv2 = d.vdev->rv2;
+  const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
   constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
-  const int nwarps = gridDim.x * kWarps;
-  for (int cell = blockIdx.x * kWarps + wid; cell < ncell_tot; cell += nwarps) {
-    const int cs = d.cell_start[cell];
-    const int ce = d.cell_start[cell + 1];
-    if (cs >= ce) continue;
-    const RepDev* R = d.reps + replica_of_cell(d, cell, nrep);
-    const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
+  // the chunk's rows cell by cell: [cs, ce) are the chunk's rows of one cell
+  for (int cs = s0; cs < s_end;) {
+    const int cell = (int)d.scell[cs];
+    const int ce = min(d.cell_start[cell + 1], s_end);
     int cx, cy, cz;
     cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
     __syncwarp();
@@ -418,27 +411,16 @@ __global__ void __launch_bounds__(kRowBlock) k_verlet_build(DevState d, int ncel
         d.drz[me] = d.dsz[i];
       }
     }
+    cs = ce;
   }
 }
 
-void launch_verlet_build(const DevState& d, int ncell_tot, int nrep, int reach, cudaStream_t st) {
-  if (ncell_tot == 0) return;
-  static int sms[64] = {};  // SMs per device ordinal
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && sms[dev] == 0)
-    cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-  const int nsm = dev >= 0 && dev < 64 && sms[dev] > 0 ? sms[dev] : 1;
-  int per_sm = 1;
+void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st) {
+  if (nblk == 0) return;
   if (reach == 2)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verlet_build<2>, kRowBlock, 0);
+    k_verlet_build<2><<<nblk, kRowBlock, 0, st>>>(d);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verlet_build<1>, kRowBlock, 0);
-  const int grid = std::min(nsm * std::max(per_sm, 1), (ncell_tot + kWarps - 1) / kWarps);
-  if (reach == 2)
-    k_verlet_build<2><<<grid, kRowBlock, 0, st>>>(d, ncell_tot, nrep);
-  else
-    k_verlet_build<1><<<grid, kRowBlock, 0, st>>>(d, ncell_tot, nrep);
+    k_verlet_build<1><<<nblk, kRowBlock, 0, st>>>(d);
 }
 
 

@@ -173,7 +173,7 @@ void launch_density(const DevState& d, int nblk, int mode, int reach, bool verle
 // marks; else the cells are swept).
 void launch_precursor(const DevState& d, int nblk, bool marks, cudaStream_t st);
 // The kept lists of every particle (when this step rebuilds).
-void launch_verlet_build(const DevState& d, int ncell_tot, int nrep, int reach, cudaStream_t st);
+void launch_verlet_build(const DevState& d, int nblk, int reach, cudaStream_t st);
 // Pass 2 (kept: pass 1 ran over the kept lists; rows: the capacity of the
 // force sums, which the FP32 pass zeroes first, since its terms arrive by
 // atomic add).
@@ -259,5 +259,8 @@ void launch_set_dynamics(const DevState& d, const double* pos, const double* vel
                          double box2, bool kept, cudaStream_t st);
 void launch_soa_to_aos(const double* x, const double* y, const double* z, const uint32_t* loc,
                        int row0, double* aos, int n, cudaStream_t st);
+void launch_gather_u32x4(const uint32_t* a, const uint32_t* b, const uint32_t* c,
+                         const uint32_t* e, const uint32_t* loc, int row0, uint32_t* out, int n,
+                         cudaStream_t st);
 
 }  // namespace idpd

@@ -33,7 +33,7 @@ EXPORTS = [
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
     "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
     "idpd_write_xyz", "idpd_list_rebuilds", "idpd_set_precursor", "idpd_precursor_count",
-    "idpd_pair_count",
+    "idpd_pair_count", "idpd_dump_xyz_async", "idpd_dump_wait",
 ]
 
 # The reference's EPI / EPJ / RESULT layouts (ptcl_class.hpp:5-174) as numpy
@@ -90,6 +90,8 @@ def load(path=LIB_PATH):
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_list_rebuilds.argtypes = [H, C.POINTER(C.c_uint64)]
     L.idpd_pair_count.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64)]
+    L.idpd_dump_xyz_async.argtypes = [H, C.c_int32, C.c_char_p, C.c_int32]
+    L.idpd_dump_wait.argtypes = [H]
     L.idpd_set_precursor.argtypes = [H, C.c_int32, C.POINTER(IdpdPrecursor)]
     L.idpd_precursor_count.argtypes = [H, C.c_int32, C.POINTER(C.c_uint64)]
     L.idpd_cell_order_noalloc.argtypes = [VP, C.c_int32, D, VP, VP, VP]
@@ -362,6 +364,16 @@ class Engine:
         n = C.c_uint64()
         self._ck(self.L.idpd_list_rebuilds(self.h, C.byref(n)), "list_rebuilds")
         return n.value
+
+    def dump_xyz_async(self, path, append=True, replica=0):
+        """Queues a traject.xyz frame of the current state (written by a host
+        thread while the steps go on)."""
+        self._ck(self.L.idpd_dump_xyz_async(self.h, replica, os.fsencode(path), 1 if append else 0),
+                 "dump_xyz_async")
+
+    def dump_wait(self):
+        """Blocks until the queued frame is written; raises on a failed frame."""
+        self._ck(self.L.idpd_dump_wait(self.h), "dump_wait")
 
     def pair_count(self, replica=0):
         """Ordered pairs within the cutoff (r < 1) of the last density pass."""

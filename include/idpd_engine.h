@@ -376,6 +376,21 @@ int idpd_write_xyz(const char* path, int32_t append, uint32_t time, int32_t n, c
                    const uint32_t* id, const uint32_t* prop, const uint32_t* amp_id,
                    const uint32_t* unit);
 
+/* ---- asynchronous trajectory frames --------------------------------------
+ * Observer::Trajectory (observer.hpp:295-305) writes traject.xyz frames with
+ * io_util::WriteXYZForm (io_util.hpp:26-31) from the host particle system.
+ * idpd_dump_xyz_async queues one such frame of replica `replica`'s current
+ * state without stopping the step loop: the rows are gathered in upload
+ * order on the handle's stream (so the frame is the state after every call
+ * queued before it), copied to pinned host memory on a second stream, and a
+ * host thread writes the frame (the idpd_write_xyz format, vel_buf = vel)
+ * while later steps run. One frame is in flight at a time: a second call
+ * first waits for the previous frame to be written. idpd_dump_wait blocks
+ * until the queued frame is on disk and returns the status of the first
+ * frame that failed since the last wait. */
+int idpd_dump_xyz_async(idpd_handle* h, int32_t replica, const char* path, int32_t append);
+int idpd_dump_wait(idpd_handle* h);
+
 /* ---- tuning --------------------------------------------------------------- */
 /* Launch and cell-grid shape of the pair passes. Every reach and launch shape
  * gives the same results bit for bit (all pair sums are fixed point); only

@@ -1,5 +1,6 @@
 """The autotuner's host logic (no GPU): choice of the fastest (reach, skin),
-skipping choices the box refuses, and the JSON cache per signature."""
+then of the fastest force-pass shape (lanes, blocks) at it, skipping choices
+the box refuses, and the JSON cache per signature."""
 import json
 
 import pytest
@@ -8,21 +9,24 @@ from implicit_dpd_gb300 import autotune as A
 
 
 class FakeEngine:
-    """Step times per (reach, skin); skins above max_skin are refused like a
-    box too small for them."""
+    """Step times per (reach, skin), scaled per force-pass shape by
+    shape_ms; skins above max_skin are refused like a box too small for
+    them."""
 
-    def __init__(self, ms, max_skin=1.0):
+    def __init__(self, ms, max_skin=1.0, shape_ms=None):
         self.ms, self.max_skin = ms, max_skin
-        self.tuning, self.steps, self.last = None, 0, 0.0
+        self.shape_ms = shape_ms or {}
+        self.tuning, self.shape, self.steps, self.last = None, None, 0, 0.0
 
-    def set_tuning(self, reach, skin=0.0):
+    def set_tuning(self, reach, skin=0.0, lanes=16, blocks=1):
         if skin > self.max_skin:
             raise ValueError("skin needs a larger box")
         self.tuning = (reach, skin)
+        self.shape = (lanes, blocks)
 
     def step(self, n):
         self.steps += n
-        self.last = self.ms[self.tuning] * n
+        self.last = self.ms[self.tuning] * self.shape_ms.get(self.shape, 1.0) * n
 
     def last_step_ms(self):
         return self.last
@@ -33,9 +37,20 @@ def test_picks_the_fastest_and_applies_it():
     ms[(1, 0.15)] = 3.2
     e = FakeEngine(ms)
     choice, times = A.tune(e)
-    assert choice == {"reach": 1, "skin": 0.15} and e.tuning == (1, 0.15)
+    assert choice == {"reach": 1, "skin": 0.15, "lanes": 16, "blocks": 1}
+    assert e.tuning == (1, 0.15) and e.shape == (16, 1)
     assert times["reach1_skin0.15"] == pytest.approx(3.2)
-    assert len(times) == len(A.DEFAULT_CHOICES)
+    assert len(times) == len(A.DEFAULT_CHOICES) + len(A.SHAPES)
+
+
+def test_then_picks_the_fastest_force_shape_at_that_reach_and_skin():
+    ms = {c: 5.0 for c in A.DEFAULT_CHOICES}
+    ms[(2, 0.2)] = 3.0
+    e = FakeEngine(ms, shape_ms={(8, 1): 0.9, (32, 1): 1.2})
+    choice, times = A.tune(e)
+    assert choice == {"reach": 2, "skin": 0.2, "lanes": 8, "blocks": 1}
+    assert e.tuning == (2, 0.2) and e.shape == (8, 1)
+    assert times["lanes8_blocks1"] == pytest.approx(2.7)
 
 
 def test_skips_choices_the_box_refuses():
@@ -43,7 +58,7 @@ def test_skips_choices_the_box_refuses():
     e = FakeEngine(ms, max_skin=0.15)
     choice, times = A.tune(e)
     assert choice["skin"] == 0.15
-    assert all(float(k.split("skin")[1]) <= 0.15 for k in times)
+    assert all(float(k.split("skin")[1]) <= 0.15 for k in times if k.startswith("reach"))
     with pytest.raises(ValueError):
         A.tune(FakeEngine(ms, max_skin=-1.0))
 
@@ -59,10 +74,13 @@ def test_cache_round_trip(tmp_path):
     assert stored[key]["reach"] == 2 and stored[key]["skin"] == 0.2
     e2 = FakeEngine(ms)
     choice, times = A.tune(e2, key=key, cache_path=path)
-    assert choice == {"reach": 2, "skin": 0.2} and times == {} and e2.steps == 0
+    assert choice == {"reach": 2, "skin": 0.2, "lanes": 16, "blocks": 1}
+    assert times == {} and e2.steps == 0 and e2.shape == (16, 1)
     ms[(1, 0.1)] = 1.0
-    choice, times = A.tune(FakeEngine(ms), key=key, cache_path=path, refresh=True)
-    assert choice == {"reach": 1, "skin": 0.1} and json.load(open(path))[key]["skin"] == 0.1
+    choice, times = A.tune(FakeEngine(ms, shape_ms={(16, 2): 0.5}), key=key, cache_path=path,
+                           refresh=True)
+    assert choice == {"reach": 1, "skin": 0.1, "lanes": 16, "blocks": 2}
+    assert json.load(open(path))[key]["skin"] == 0.1 and json.load(open(path))[key]["blocks"] == 2
 
 
 def test_signature_groups_close_systems():

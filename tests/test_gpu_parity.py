@@ -2,7 +2,8 @@
 
 Integer parts are bit-exact (Saru u32, cell ids, sorted order, pair sets,
 fixed-point sums). Forces meet the spec bar FORCE_TOL (relative 1e-5
-against the FP64 oracle, see helpers.rel_force_err); densities the same bar.
+against the FP64 oracle, see helpers.rel_force_err); densities and the
+per-particle pair virial (press) the same bar.
 """
 import os
 
@@ -85,7 +86,7 @@ def test_force_pass_matches_oracle_mdpd():
     worst, agg = rel_force_err(got["acc"], acc)
     assert worst < FORCE_TOL, (worst, agg)
     aux = e.download_aux(density=False, press=True)
-    assert rel_force_err(aux["press"], press)[0] < 1e-4
+    assert rel_force_err(aux["press"], press)[0] < FORCE_TOL
 
 
 def test_force_matches_reference_golden_vectors():
@@ -153,7 +154,7 @@ def test_large_pair_terms_take_the_64bit_sums(a):
     got = e.download()
     assert rel_force_err(got["acc"], acc)[0] < FORCE_TOL
     aux = e.download_aux(press=True)
-    assert np.abs(aux["press"] - press).max() / np.abs(press).max() < 1e-4
+    assert rel_force_err(aux["press"], press)[0] < FORCE_TOL
     s1, ref = _step_compare(p, st, 0, [], 0)
     assert rel_force_err(s1["acc"], ref["acc"])[0] < FORCE_TOL
     assert np.array_equal(s1["pos"], ref["pos"])
