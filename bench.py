@@ -566,13 +566,18 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     eb.step(3)
     dist.barrier()
     eb.step(steps)
-    graph_ms = eb.last_step_ms() / steps
     batched = n_tot * steps / (dist.max(eb.last_step_ms()) * 1e-3)
     # what one persistent launch could save at most: the graph step's time
-    # beyond its kernels' own times (CUDA events of un-graphed profile steps,
-    # median of 5; the events add their own gaps, so this bounds from above)
-    prof = [eb.profile_step() for _ in range(5)]
-    kernels_ms = sum(statistics.median(p_[k] for p_ in prof) for k in prof[0])
+    # beyond its kernels' own times. Compared at skin 0, where every step does
+    # the same work (cells and all passes): 20 graph steps against the mean of
+    # 10 un-graphed profile steps (CUDA events between kernels; the events add
+    # gaps of their own, so the difference is a lower bound on the gaps)
+    eb.set_tuning(reach, 0.0)
+    eb.step(3)
+    eb.step(20)
+    graph_ms = eb.last_step_ms() / 20
+    prof = [eb.profile_step() for _ in range(10)]
+    kernels_ms = sum(statistics.mean(p_[k] for p_ in prof) for k in prof[0])
     eb.close()
     singles = []
     for i in mine:
@@ -596,8 +601,9 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
             "steps": steps, "tuning": {"reach": reach, "skin": skin},
             "batched": batched, "one_at_a_time": one_at_a_time,
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
-            "graph_ms_per_step": graph_ms, "kernels_ms_per_step": kernels_ms,
-            "launch_gap_share": max(0.0, graph_ms - kernels_ms) / graph_ms,
+            "launch_gaps": {"tuning": {"reach": reach, "skin": 0.0}, "graph_ms_per_step": graph_ms,
+                            "kernels_ms_per_step": kernels_ms,
+                            "share": max(0.0, graph_ms - kernels_ms) / graph_ms},
             "partition": {"ranks": world, "rule": "greedy LPT on particle counts",
                           "replicas_per_rank": [len(p) for p in parts],
                           "particles_per_rank": loads, "imbalance": imbalance(loads)},
