@@ -89,7 +89,8 @@ def workload_desc(n, n_amp, box=BOX, layers=N_LAYERS):
                         "{:g}x{:g}x{:g} box, ".format(*box) +
                         "reference MDPD form (chi 30, kappa 100, rho_co 40, vbb 0.1), sigma 3, "
                         "dt 0.005, cf_s 50, cf_b 10; timed after the equilibration steps, when "
-                        "the bilayers have compacted to ~130 in-range neighbours per bead"),
+                        "the bilayers have compacted to ~150 ordered pairs within the cutoff per "
+                        "bead"),
         "n_particles": int(n),
         "n_molecules": int(n_amp),
         "l2": ("inputs larger than L2: the pair passes read posf, poslo, velf, densf and the "
@@ -829,6 +830,7 @@ def run_engine(args, rank, world, local_rank):
                                                equilibration_s=t_eq, tuning=reach,
                                                autotune_ms_per_step=tune_ms,
                                                list_rebuilds_in_timed_steps=rebuilds,
+                                               pairs_per_bead=pairs / n,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "fp64_same_algorithm": fp64_same,
