@@ -96,8 +96,10 @@ __global__ void __launch_bounds__(kRowBlock) k_drift_disp(DevState d) {
   if (threadIdx.x == 0) {
     float b = 0.0f;
     for (int w = 0; w < kRowBlock / 32; w++) b = fmaxf(b, wmax[w]);
-    // non-negative floats order like their bit patterns
-    if (b > 0.0f) atomicMax(&d.vdev->maxd2, __float_as_uint(b));
+    // non-negative floats order like their bit patterns; the running maximum
+    // is read first, so only blocks that raise it take the (single-address) atomic
+    const unsigned int bb = __float_as_uint(b);
+    if (b > 0.0f && bb > *(volatile unsigned int*)&d.vdev->maxd2) atomicMax(&d.vdev->maxd2, bb);
   }
 }
 
