@@ -247,14 +247,15 @@ def profiled_traffic(name):
 
 
 def equilibrated_patch(threads, equil=2000):
-    """One bilayer of an 8 x 8 x 4.8 periodic patch of membrane_1m taken
-    through `equil` oracle steps (the compaction the timed GPU state went
-    through). Returns (state, patch box, molecules, params)."""
+    """An 8 x 8 x 48 periodic column of membrane_1m (the same ten stacked
+    bilayers and box height, 15,360 beads) taken through `equil` oracle steps:
+    the compaction the timed GPU state went through, so the CPU sample has the
+    GPU state's pairs per bead. Returns (state, patch box, molecules, params)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
 
-    small = np.array([8.0, 8.0, BOX[2] / N_LAYERS])
-    st, n_amp, rp = workload(box=small, layers=1, seed=7)
+    small = np.array([8.0, 8.0, BOX[2]])
+    st, n_amp, rp = workload(box=small, layers=N_LAYERS, seed=7)
     p = O.derive_params(rp)
     p.seed, p.time = 1, 1
     st["topol"], st["cf_bend"] = O.build_topology(st["amp_id"], st["unit"], n_amp, [], p.cf_b,
@@ -266,8 +267,8 @@ def equilibrated_patch(threads, equil=2000):
 
 
 def tile_patch(patch, reps):
-    """reps = (nx, ny) periodic copies of the equilibrated patch side by side:
-    a bilayer of membrane_1m of (8 nx) x (8 ny) x 4.8."""
+    """reps = (nx, ny) periodic copies of the equilibrated column side by side:
+    a (8 nx) x (8 ny) x 48 section of membrane_1m."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
 
@@ -284,23 +285,21 @@ def tile_patch(patch, reps):
     return big, n_amp_big, pb, box
 
 
-def equilibrated_slab(threads, equil=2000):
-    """A bounded CPU sample of the equilibrated workload: the equilibrated
-    patch tiled 8 x 8 into one bilayer period of membrane_1m (64 x 64 x 4.8,
-    98,304 beads)."""
-    big, n_amp_big, pb, _ = tile_patch(equilibrated_patch(threads, equil), (8, 8))
-    return big, n_amp_big, pb
-
-
-def cpu_baseline(min_seconds=10.0, max_steps=50):
-    """The C oracle (the reference's CPU algorithm, FP64) on a bounded sample
-    of the equilibrated workload (one bilayer period, 98,304 beads), every host
-    thread."""
+def cpu_baseline(state, n_amp, rp, time_step, min_seconds=10.0, max_steps=50):
+    """The C oracle (the reference's CPU algorithm, FP64) timed on the GPU's own
+    timed state (the whole workload, downloaded after the timed steps: the same
+    configuration and pairs per bead as the GPU's figure), every host thread,
+    for about min_seconds, with the parity build and with the reference's
+    production flags."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
 
     threads = os.cpu_count() or 1
-    st, n_amp, p = equilibrated_slab(threads)
+    p = O.derive_params(rp)
+    p.seed, p.time = 12345, int(time_step)
+    st = {k: np.array(state[k], copy=True) for k in ("pos", "vel", "acc", "id", "prop")}
+    st["topol"], st["cf_bend"] = O.build_topology(state["amp_id"], state["unit"], n_amp, [],
+                                                  p.cf_b, p.cf_b_rigid)
     n = len(st["pos"])
     pairs = O.pair_count(p, st["pos"], threads) / n
 
@@ -322,10 +321,9 @@ def cpu_baseline(min_seconds=10.0, max_steps=50):
     steps, dt = timed(False)
     steps_f, dt_f = timed(True)
     out = {"value": n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-           "sample": f"{steps} MD steps (drift, density, force, bonded, kick) of one equilibrated "
-                     f"bilayer period of the workload (64x64x4.8, {n} beads, {pairs:.1f} ordered "
-                     f"pairs within the cutoff per bead), FP64 C oracle (-O2, no contraction), "
-                     f"OpenMP",
+           "sample": f"{steps} MD steps (drift, density, force, bonded, kick) of the GPU's timed "
+                     f"state itself ({n} beads, {pairs:.1f} ordered pairs within the cutoff per "
+                     f"bead), FP64 C oracle (-O2, no contraction), OpenMP",
            "pairs_per_bead": pairs,
            "production_flags": {"value": n * steps_f / dt_f, "unit": "particle-steps/s",
                                 "steps": steps_f,
@@ -346,15 +344,15 @@ def run_reference(args, rank, world, budget_s=90.0):
 
     threads = os.cpu_count() or 1
     patch = equilibrated_patch(threads)
-    # rate of the oracle on one bilayer period, then the sample that fits the budget
-    probe, _, pp, _ = tile_patch(patch, (8, 8))
+    # rate of the oracle on a 24 x 16 x 48 section, then the sample that fits the budget
+    probe, _, pp, _ = tile_patch(patch, (3, 2))
     t0 = time.perf_counter()
     O.md_step(pp, probe, nthreads=threads)
     rate = len(probe["pos"]) / (time.perf_counter() - t0)
     per_step = budget_s / max(1, args.steps + args.warmup)
     tiles = int(min(64, max(1, rate * per_step // len(patch[0]["pos"]))))
     ny = min(8, tiles)
-    nx = max(1, tiles // ny)
+    nx = max(1, min(8, tiles // ny))
     st, n_amp, p, box = tile_patch(patch, (nx, ny))
     for _ in range(args.warmup):
         O.md_step(p, st, nthreads=threads)
@@ -366,7 +364,7 @@ def run_reference(args, rank, world, budget_s=90.0):
     value = n * args.steps / dt
     pairs = O.pair_count(p, st["pos"], threads) / n
     sample = (f"each step one MD step (drift, density, force, bonded, kick) of an equilibrated "
-              f"bilayer patch of membrane_1m ({box[0]:g}x{box[1]:g}x{box[2]:g}, {n} beads, "
+              f"section of membrane_1m (the ten stacked bilayers, {box[0]:g}x{box[1]:g}x{box[2]:g}, {n} beads, "
               f"{pairs:.1f} ordered pairs within the cutoff per bead), FP64 C oracle of the "
               f"reference algorithm, OpenMP")
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -821,7 +819,10 @@ def run_engine(args, rank, world, local_rank):
                if not args.no_replicas else None)
     reaction = reaction_bench(reach, device=local_rank) if not args.no_reaction else None
     liquid = liquid_bench(device=local_rank) if not args.no_liquid else None
-    cpu = cpu_baseline() if (rank == 0 and world == 1 and not args.no_cpu) else None
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        timed_state = e.download()
+        cpu = cpu_baseline(timed_state, n_amp, rp, e.get_params().time)
     n_reorders = args.steps // 100
     out = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
