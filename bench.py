@@ -535,7 +535,8 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
     A in [-50, -30], B = 25, densities 5-7): all of a rank's replicas in one
     handle, one CUDA graph per step, against the same replicas stepped one
-    handle at a time with the same (reach, skin), tuned on the batch. On
+    handle at a time with the same tuning (reach, skin and force-pass shape,
+    picked by the package's tuner on the batch). On
     several ranks the replicas are dealt out by LPT on their particle counts
     (no exchange while stepping); the job's rate is all particles x steps
     over the slowest rank's time. Returns particle-steps/s of both forms."""
@@ -554,14 +555,9 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
         eb.set_params(params[i], k)
         eb.upload(reps[i]["state"], k)
     eb.step(3)
-    times = {}
-    for reach, skin in [(1, 0.0), (1, 0.2), (1, 0.3)]:
-        eb.set_tuning(reach, skin)
-        eb.step(2)
-        eb.step(20)
-        times[(reach, skin)] = eb.last_step_ms()
-    reach, skin = min(times, key=times.get)
-    eb.set_tuning(reach, skin)
+    # the package's tuner on the batch: (reach, skin), then the force pass's shape
+    tuned, _ = autotune(eb, steps=20)
+    reach, skin, lanes, blocks = tuned["reach"], tuned["skin"], tuned["lanes"], tuned["blocks"]
     eb.step(3)
     dist.barrier()
     eb.step(steps)
@@ -583,7 +579,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
         e = Engine(device=device)
         e.set_params(params[i])
         e.upload(reps[i]["state"])
-        e.set_tuning(reach, skin)
+        e.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
         e.step(3)
         singles.append(e)
     import torch
@@ -597,7 +593,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     for e in singles:
         e.close()
     return {"workload": "mdpd_replicas_256", "n_replicas": n_rep, "n_particles": int(n_tot),
-            "steps": steps, "tuning": {"reach": reach, "skin": skin},
+            "steps": steps, "tuning": tuned,
             "batched": batched, "one_at_a_time": one_at_a_time,
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
             "launch_gaps": {"tuning": {"reach": reach, "skin": 0.0}, "graph_ms_per_step": graph_ms,
