@@ -54,12 +54,13 @@ STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
 # (the Saru hash and draws) + 5 SFU (sqrt r, rcp, sqrt w, log, cos); the
 # density pass ~12 FP32 + 1 SFU.
 OPS_PER_ORDERED_PAIR = {"force": 134, "density": 13}
-KERNELS_PER_STEP = 15          # drift_bin, scan x3, scatter, cell_sort, pack, density,
-                               # density finalize, force, bonded_kick, cmdrift x3, time
-KERNELS_PER_KEPT_STEP = 18     # drift_disp, rebuild decision, gated bin, gated scan x3,
+KERNELS_PER_STEP = 16          # drift_bin, scan x3, scatter, cell_sort, pack, density,
+                               # density finalize, force, force walk, bonded_kick,
+                               # cmdrift x3, time
+KERNELS_PER_KEPT_STEP = 20     # drift_disp, rebuild decision, gated bin, gated scan x3,
                                # gated scatter / cell_sort / pack, gated list build,
-                               # density, density finalize, force, bonded_kick, cmdrift x3,
-                               # time
+                               # density (kept lists, overflowed kept lists), density
+                               # finalize, force, force walk, bonded_kick, cmdrift x3, time
 KERNELS_PER_REORDER = 4        # gather, topology, identity, loc
 
 

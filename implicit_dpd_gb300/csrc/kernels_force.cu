@@ -299,9 +299,7 @@ struct ForceWarpSmem {
 
 
 
-size_t force_smem_bytes(int fb) {
-  return (size_t)fb * sizeof(ForceBlockSmem) + (size_t)fb * kWarps * sizeof(ForceWarpSmem);
-}
+size_t force_smem_bytes(int fb) { return (size_t)fb * sizeof(ForceBlockSmem); }
 
 // Each pair is evaluated once, by the particle that owns it (owns()), and
 // its term goes to both particles (Newton's third law in exact fixed point: the
@@ -310,48 +308,29 @@ size_t force_smem_bytes(int fb) {
 // at a time, LP lanes each, over their pass-1 lists (owned pairs only),
 // grouped by list length (the chunk sorted by length, neighbours in that
 // order share a warp) so that the groups run about as long; each lane reads
-// its next list entry one round ahead. A CTA takes blockDim / 128 consecutive
-// 128-row blocks of the row-block map (more rows per CTA keep more of their
-// shared neighbours in one SM's L1). The sums start at zero (launch_force)
-// and every term arrives by atomic add. A particle whose list overflowed
-// walks its cells again with the whole warp and queues the in-range pairs in
-// shared memory; a particle with a term outside the 32-bit parts' range is
-// summed again in 64 bits (its own side only). One launch per pair form
-// present: a warp whose replica has another form returns at once.
+// its next list entry one round ahead. The sums start at zero (launch_force)
+// and every term arrives by atomic add. A particle with a term outside the
+// 32-bit parts' range is summed again in 64 bits (its own side only). A
+// particle whose list overflowed is left to k_force_walk, so that this pass
+// keeps no walk state: no spills at 64 registers, and only the replica
+// tables in shared memory, which leaves the SM's L1 the room to cache the
+// other particles' rows (with the walk's 7.6 KB of shared memory per CTA in
+// the same kernel the pass took 1.15 ms instead of 1.08 on membrane_1m).
+// One launch per pair form present: a warp whose replica has another form
+// returns at once.
+//
+// Pass 2 over the rows s0 .. s0 + 31 of replica r (one warp's chunk), the
+// particles whose pass-1 list fit: G particles at a time, LP lanes each.
 template <int REACH, bool PRESS, int FORM, int LP>
-__global__ void __launch_bounds__(1024, 1) k_force_f32(DevState d, int kept, int nblk) {
+__device__ __forceinline__ void force_rows(const DevState& d, int s0, int r, const RepDev* R,
+                                           const PairTables& T, const OffTable& OT, int lane) {
   constexpr int G = 32 / LP;  // particles per warp at a time
-  extern __shared__ __align__(16) unsigned char force_smem[];
-  const int fb = blockDim.x >> 7;  // 128-row blocks of this CTA
-  ForceBlockSmem* BS = reinterpret_cast<ForceBlockSmem*>(force_smem);
-  ForceWarpSmem* WS = reinterpret_cast<ForceWarpSmem*>(force_smem + fb * sizeof(ForceBlockSmem));
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int rbl = wid / kWarps;              // the warp's row block within the CTA
-  const int rb = blockIdx.x * fb + rbl;      // in the row-block map
-  const int r = rb < nblk ? d.blk_rep[rb] : 0;
-  const RepDev* R = d.reps + r;
-  if (rb < nblk) {
-    const int tb = threadIdx.x & (kRowBlock - 1);
-    if (tb < 9) fill_pair_table(BS[rbl].T, *R, tb);
-    if (tb < 64) fill_off_table(BS[rbl].OT, *R, tb);
-  }
-  __syncthreads();
-  if (rb >= nblk || R->form != FORM) return;
-  const PairTables& T = BS[rbl].T;
-  const OffTable& OT = BS[rbl].OT;
   const int h = lane / LP, sl = lane % LP;
-  SegTable& S = WS[wid].seg;
-  uint32_t* QT = WS[wid].qt;
-  uint32_t* QC = WS[wid].qc;
-  const int s0 = d.blk_row[rb] + 32 * (wid % kWarps);
   const int s_end = min(s0 + 32, R->row_off + R->n);
   if (s0 >= s_end) return;
   PairI I;
   I.seed = R->seed + d.rep_time[r];
-  constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
-  const uint32_t lt_mask = (1u << lane) - 1u;
   constexpr uint32_t group_mask = LP == 32 ? 0xffffffffu : ((1u << LP) - 1u);
-  int cached = -1;
   // the chunk's rows sorted by the length of their lists (rows past the end
   // and overflowed lists count 0): key = length << 5 | row - s0
   uint32_t key;
@@ -407,90 +386,22 @@ __global__ void __launch_bounds__(1024, 1) k_force_f32(DevState d, int kept, int
         }
       }
     }
-    // ---- the particles that need 64-bit sums, one at a time, whole warp
-    uint32_t slow = __ballot_sync(0xffffffffu, sl == 0 && act && (cnt == kNbrFallback || !ok));
+    // ---- a term outside the parts' range: the particle's own side again in
+    // 64 bits, one particle at a time, whole warp (the other particles'
+    // shares are already in memory)
+    uint32_t slow = __ballot_sync(0xffffffffu, sl == 0 && act && cnt != kNbrFallback && !ok);
     while (slow) {
       const int hs = (__ffs(slow) - 1) / LP;
       slow &= slow - 1;
       const int ss = __shfl_sync(0xffffffffu, s, LP * hs);
       load_row(I, d, ss);
       I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
-      const uint32_t c2 = d.nbn[ss];
-      if (c2 != kNbrFallback) {  // a term outside the parts' range: the own side again
-        const uint32_t* l2 = d.nbl + (size_t)ss * kNbrCap;
-        const int n2 = (int)c2;
-        for (int k = lane; k < n2; k += 32) {
-          int t, dx, dy, dz;
-          read_entry(l2[k], t, dx, dy, dz);
-          eval_pair<PRESS, FORM, false>(d, R, T, I, t, dx, dy, dz);
-        }
-      } else {  // the list did not fit: walk the cells
-        const int cell = (int)d.scell[ss];
-        if (cell != cached) {  // the segments of the particle's cell (only this path walks cells)
-          int cx, cy, cz;
-          cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
-          __syncwarp();
-          build_segments(S, d, R, cx, cy, cz, lane);
-          __syncwarp();
-          cached = cell;
-        }
-        int qn = 0;
-#pragma unroll 1
-        for (int g = 0; g < nseg; g++) {
-          const int tb = S.tb[g], te = S.te[g];
-          if (tb >= te) continue;
-          const int code = S.code[g];
-          int b[2 * REACH];
-#pragma unroll
-          for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
-          const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
-          const float by = I.pi.y - (float)dy * R->cs_f[1], bz = I.pi.z - (float)dz * R->cs_f[2];
-          for (int t0 = tb; t0 < te; t0 += 32) {
-            const int t = t0 + lane;
-            bool in = false, own = false;
-            int dx = 0;
-            bool near = false;
-            if (t < te && t != ss) {
-              const float4 pj = __ldg(d.posf + t);
-              dx = fx0 + frame_step<REACH>(t, b);
-              const float ex = (I.pi.x - (float)dx * R->cs_f[0]) - pj.x, ey = by - pj.y,
-                          ez = bz - pj.z;
-              const float dr2 = ex * ex + ey * ey + ez * ez;
-              in = dr2 < 1.0f;
-              near = fabsf(dr2 - 1.0f) <= kGuard;
-              own = owns(dx, kept ? d.okey[t] : pj.x, kept ? d.okey[ss] : I.pi.x, t, ss);
-            }
-            if (__any_sync(0xffffffffu, near) && near) {
-              in = exact_dr2(d, R, d.perm[ss], d.perm[t]) < 1.0;
-            }
-            in = in && own;  // the pairs this particle owns
-            const uint32_t mask = __ballot_sync(0xffffffffu, in);
-            if (in) {
-              const int pos = qn + __popc(mask & lt_mask);
-              QT[pos] = (uint32_t)t;
-              QC[pos] = pack_code(dx, code);
-            }
-            qn += __popc(mask);
-            if (qn >= 32) {
-              __syncwarp();
-              const PairCode pc = unpack_code(QC[lane]);
-              eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
-              __syncwarp();
-              if (lane < qn - 32) {
-                QT[lane] = QT[32 + lane];
-                QC[lane] = QC[32 + lane];
-              }
-              __syncwarp();
-              qn -= 32;
-            }
-          }
-        }
-        __syncwarp();
-        if (lane < qn) {
-          const PairCode pc = unpack_code(QC[lane]);
-          eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
-        }
-        __syncwarp();
+      const uint32_t* l2 = d.nbl + (size_t)ss * kNbrCap;
+      const int n2 = (int)d.nbn[ss];
+      for (int k = lane; k < n2; k += 32) {
+        int t, dx, dy, dz;
+        read_entry(l2[k], t, dx, dy, dz);
+        eval_pair<PRESS, FORM, false>(d, R, T, I, t, dx, dy, dz);
       }
       const long long fx = warp_sum_ll(I.fx), fy = warp_sum_ll(I.fy), fz = warp_sum_ll(I.fz);
       long long px = 0, py = 0, pz = 0;
@@ -515,18 +426,177 @@ __global__ void __launch_bounds__(1024, 1) k_force_f32(DevState d, int kept, int
   }
 }
 
+// Pass 2 for the particles of the chunk s0 .. s0 + 31 whose pass-1 list did
+// not fit (more than kNbrCap owned pairs, only at extreme densities): one at
+// a time, the whole warp walks the particle's cells again and queues its
+// owned in-range pairs in shared memory; each term goes to both particles.
+template <int REACH, bool PRESS, int FORM>
+__device__ __forceinline__ void force_walk_rows(const DevState& d, int kept, int s0, int r,
+                                                const RepDev* R, const PairTables& T,
+                                                ForceWarpSmem& W, int lane) {
+  const int s_end = min(s0 + 32, R->row_off + R->n);
+  if (s0 >= s_end) return;
+  SegTable& S = W.seg;
+  uint32_t* QT = W.qt;
+  uint32_t* QC = W.qc;
+  PairI I;
+  I.seed = R->seed + d.rep_time[r];
+  constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  int cached = -1;
+  uint32_t slow = __ballot_sync(0xffffffffu, s0 + lane < s_end && d.nbn[s0 + lane] == kNbrFallback);
+  while (slow) {
+    const int ss = s0 + __ffs(slow) - 1;
+    slow &= slow - 1;
+    load_row(I, d, ss);
+    I.fx = I.fy = I.fz = I.px = I.py = I.pz = 0;
+    const int cell = (int)d.scell[ss];
+    if (cell != cached) {  // the segments of the particle's cell (only this path walks cells)
+      int cx, cy, cz;
+      cell_xyz(cell - R->cell_off, R->nc, cx, cy, cz);
+      __syncwarp();
+      build_segments(S, d, R, cx, cy, cz, lane);
+      __syncwarp();
+      cached = cell;
+    }
+    int qn = 0;
+#pragma unroll 1
+    for (int g = 0; g < nseg; g++) {
+      const int tb = S.tb[g], te = S.te[g];
+      if (tb >= te) continue;
+      const int code = S.code[g];
+      int b[2 * REACH];
+#pragma unroll
+      for (int q = 0; q < 2 * REACH; q++) b[q] = S.bnd[g][q];
+      const int fx0 = (code & 7) - 4, dy = ((code >> 3) & 7) - 4, dz = ((code >> 6) & 7) - 4;
+      const float by = I.pi.y - (float)dy * R->cs_f[1], bz = I.pi.z - (float)dz * R->cs_f[2];
+      for (int t0 = tb; t0 < te; t0 += 32) {
+        const int t = t0 + lane;
+        bool in = false, own = false;
+        int dx = 0;
+        bool near = false;
+        if (t < te && t != ss) {
+          const float4 pj = __ldg(d.posf + t);
+          dx = fx0 + frame_step<REACH>(t, b);
+          const float ex = (I.pi.x - (float)dx * R->cs_f[0]) - pj.x, ey = by - pj.y,
+                      ez = bz - pj.z;
+          const float dr2 = ex * ex + ey * ey + ez * ez;
+          in = dr2 < 1.0f;
+          near = fabsf(dr2 - 1.0f) <= kGuard;
+          own = owns(dx, kept ? d.okey[t] : pj.x, kept ? d.okey[ss] : I.pi.x, t, ss);
+        }
+        if (__any_sync(0xffffffffu, near) && near) {
+          in = exact_dr2(d, R, d.perm[ss], d.perm[t]) < 1.0;
+        }
+        in = in && own;  // the pairs this particle owns
+        const uint32_t mask = __ballot_sync(0xffffffffu, in);
+        if (in) {
+          const int pos = qn + __popc(mask & lt_mask);
+          QT[pos] = (uint32_t)t;
+          QC[pos] = pack_code(dx, code);
+        }
+        qn += __popc(mask);
+        if (qn >= 32) {
+          __syncwarp();
+          const PairCode pc = unpack_code(QC[lane]);
+          eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+          __syncwarp();
+          if (lane < qn - 32) {
+            QT[lane] = QT[32 + lane];
+            QC[lane] = QC[32 + lane];
+          }
+          __syncwarp();
+          qn -= 32;
+        }
+      }
+    }
+    __syncwarp();
+    if (lane < qn) {
+      const PairCode pc = unpack_code(QC[lane]);
+      eval_pair<PRESS, FORM, true>(d, R, T, I, (int)QT[lane], pc.dx, pc.dy, pc.dz);
+    }
+    __syncwarp();
+    const long long fx = warp_sum_ll(I.fx), fy = warp_sum_ll(I.fy), fz = warp_sum_ll(I.fz);
+    long long px = 0, py = 0, pz = 0;
+    if (PRESS) {
+      px = warp_sum_ll(I.px);
+      py = warp_sum_ll(I.py);
+      pz = warp_sum_ll(I.pz);
+    }
+    if (lane == 0) {
+      long long* q = d.fq + 4 * (size_t)ss;
+      red_add(q, fx);
+      red_add(q + 1, fy);
+      red_add(q + 2, fz);
+      if (PRESS) {
+        long long* pq = d.pq + 4 * (size_t)ss;
+        red_add(pq, px);
+        red_add(pq + 1, py);
+        red_add(pq + 2, pz);
+      }
+    }
+  }
+}
+
+// Pass 2, grid order: CTA b takes row blocks b fb .. b fb + fb - 1, one warp
+// per 32-row chunk. Its shared memory is the replica tables only (1.2 KB per
+// row block), which leaves most of the SM's 256 KB of L1 and shared memory
+// to the L1 that caches the other particles' rows.
+template <int REACH, bool PRESS, int FORM, int LP>
+__global__ void __launch_bounds__(1024, 1) k_force_f32(DevState d, int nblk) {
+  extern __shared__ __align__(16) unsigned char force_smem[];
+  ForceBlockSmem* BS = reinterpret_cast<ForceBlockSmem*>(force_smem);
+  const int fb = blockDim.x >> 7;  // 128-row blocks of this CTA
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int rbl = wid / kWarps;              // the warp's row block within the CTA
+  const int rb = blockIdx.x * fb + rbl;      // in the row-block map
+  const int r = rb < nblk ? d.blk_rep[rb] : 0;
+  const RepDev* R = d.reps + r;
+  if (rb < nblk) {
+    const int tb = threadIdx.x & (kRowBlock - 1);
+    if (tb < 9) fill_pair_table(BS[rbl].T, *R, tb);
+    if (tb < 64) fill_off_table(BS[rbl].OT, *R, tb);
+  }
+  __syncthreads();
+  if (rb >= nblk || R->form != FORM) return;
+  force_rows<REACH, PRESS, FORM, LP>(d, d.blk_row[rb] + 32 * (wid % kWarps), r, R, BS[rbl].T,
+                                     BS[rbl].OT, lane);
+}
+
+// Pass 2 of the particles whose list overflowed (force_walk_rows), one warp
+// per 32-row chunk, 128-row blocks per CTA; a chunk without such a particle
+// costs one read of its list lengths.
+template <int REACH, bool PRESS, int FORM>
+__global__ void __launch_bounds__(kRowBlock) k_force_walk(DevState d, int kept, int nblk) {
+  __shared__ ForceBlockSmem B;
+  __shared__ ForceWarpSmem W[kWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int rb = blockIdx.x;
+  const int r = d.blk_rep[rb];
+  const RepDev* R = d.reps + r;
+  if (threadIdx.x < 9) fill_pair_table(B.T, *R, threadIdx.x);
+  __syncthreads();
+  if (R->form != FORM) return;
+  force_walk_rows<REACH, PRESS, FORM>(d, kept, d.blk_row[rb] + 32 * wid, r, R, B.T, W[wid], lane);
+}
+
 // Pass 2 of one pair form: the shape of the tuning (lanes per particle,
 // row blocks per CTA); the observation steps (PRESS) run 16 lanes, one row
 // block per CTA.
+template <int REACH, int FORM, bool PRESS, int LP>
+void launch_force_kernel(const DevState& d, int nblk, int kept, int fb, cudaStream_t st) {
+  k_force_f32<REACH, PRESS, FORM, LP>
+      <<<(nblk + fb - 1) / fb, kRowBlock * fb, force_smem_bytes(fb), st>>>(d, nblk);
+  k_force_walk<REACH, PRESS, FORM><<<nblk, kRowBlock, 0, st>>>(d, kept, nblk);
+}
+
 template <int FORM, bool PRESS, int LP>
 void launch_force_shape(const DevState& d, int nblk, int reach, int kept, int fb,
                         cudaStream_t st) {
-  const int grid = (nblk + fb - 1) / fb;
-  const size_t smem = force_smem_bytes(fb);
   if (reach == 2)
-    k_force_f32<2, PRESS, FORM, LP><<<grid, kRowBlock * fb, smem, st>>>(d, kept, nblk);
+    launch_force_kernel<2, FORM, PRESS, LP>(d, nblk, kept, fb, st);
   else
-    k_force_f32<1, PRESS, FORM, LP><<<grid, kRowBlock * fb, smem, st>>>(d, kept, nblk);
+    launch_force_kernel<1, FORM, PRESS, LP>(d, nblk, kept, fb, st);
 }
 
 template <int FORM>

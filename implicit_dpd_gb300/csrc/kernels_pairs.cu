@@ -33,15 +33,29 @@ namespace idpd {
 // dsum as well; k_dens_finalize turns them into the FP32 densities.
 // With MARKS, the precursor conversion's marks (phit): a pair of prop_from
 // and prop_near within the cutoff marks the prop_from particle.
-template <int REACH, bool VERLET, bool MARKS>
-__global__ void __launch_bounds__(kRowBlock, (VERLET && (REACH == 2 || MARKS)) ? 8 : 10) k_density_f32(DevState d) {
-  __shared__ SegTable seg[kWarps];
-  __shared__ uint32_t lst[kWarps][kNbrCap];
+//
+// Three forms (MODE): kDensSweep sweeps the cells of every row (no kept
+// lists); kDensKept takes the rows whose kept list fit and uses no shared
+// memory, which leaves the SM's L1 the room to cache the candidates' rows;
+// kDensKeptOver takes the rows whose kept list did not fit and sweeps their
+// cells (the ownership of the kept lists). The two kept-list forms run one
+// after the other (with the sweep's 13.8 KB of shared memory per CTA in the
+// kept-list kernel, pass 1 took 0.70 ms instead of 0.65 on membrane_1m). The sweeping forms keep per warp the neighbour segments
+// and a list buffer in dynamic shared memory (dens_sweep_smem_bytes).
+enum { kDensSweep = 0, kDensKept = 1, kDensKeptOver = 2 };
+constexpr size_t dens_sweep_smem_bytes() {
+  return kWarps * (sizeof(SegTable) + kNbrCap * sizeof(uint32_t));
+}
+
+template <int REACH, int MODE, bool MARKS>
+__global__ void __launch_bounds__(kRowBlock, (MODE != kDensSweep && (REACH == 2 || MARKS)) ? 8 : 10) k_density_f32(DevState d) {
+  constexpr bool VERLET = MODE != kDensSweep;
+  extern __shared__ __align__(16) unsigned char dens_smem[];
   const int r = d.blk_rep[blockIdx.x];
   const RepDev* R = d.reps + r;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  SegTable& S = seg[wid];
-  uint32_t* L = lst[wid];
+  SegTable& S = reinterpret_cast<SegTable*>(dens_smem)[wid];
+  uint32_t* L = reinterpret_cast<uint32_t*>(dens_smem + kWarps * sizeof(SegTable)) + wid * kNbrCap;
   const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
   const int s_end = min(s0 + 32, R->row_off + R->n);
   const bool warren = R->form == IDPD_FORM_WARREN_K;
@@ -53,7 +67,7 @@ __global__ void __launch_bounds__(kRowBlock, (VERLET && (REACH == 2 || MARKS)) ?
   constexpr int nseg = 2 * (2 * REACH + 1) * (2 * REACH + 1);
   const uint32_t lt_mask = (1u << lane) - 1u;
   int cached = -1;
-  for (int s = s0; s < s_end; s++) {
+  auto row = [&](const int s) {
     const float4 pi = d.posf[s];
     const uint32_t si = d.perm[s], pri = fbits(pi.w);
     const float ki = VERLET ? d.okey[s] : pi.x;  // the ownership key of the step
@@ -98,7 +112,7 @@ __global__ void __launch_bounds__(kRowBlock, (VERLET && (REACH == 2 || MARKS)) ?
     const uint32_t nv = VERLET ? (uint32_t)d.vn[s] : kNbrFallback;
     bool fits = true;
     bool swept = true;  // the pairs came from a sweep of the cells (list out below)
-    if (VERLET && nv != kNbrFallback) {
+    if constexpr (MODE == kDensKept) {
       // ---- the particle's kept list: test, weight and list out in one pass
       swept = false;
       const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
@@ -236,6 +250,17 @@ __global__ void __launch_bounds__(kRowBlock, (VERLET && (REACH == 2 || MARKS)) ?
       if (MARKS && hit) d.phit[s] = 1;
     }
     __syncwarp();
+  };
+  if constexpr (MODE == kDensKeptOver) {
+    // the few rows whose kept list did not fit: lane k tests row s0 + k
+    uint32_t rows = __ballot_sync(0xffffffffu, s0 + lane < s_end && d.vn[s0 + lane] == kNbrFallback);
+    while (rows) {
+      row(s0 + __ffs(rows) - 1);
+      rows &= rows - 1;
+    }
+  } else {
+    for (int s = s0; s < s_end; s++)
+      if (MODE == kDensSweep || d.vn[s] != kNbrFallback) row(s);
   }
 }
 
@@ -482,16 +507,23 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
   if (s < R->row_off + R->n) d.npair[s] = density_f64_row(d, r, s, R);
 }
 
+template <int REACH, bool MARKS>
+void launch_density_reach(const DevState& d, int nblk, bool verlet, cudaStream_t st) {
+  constexpr size_t sm = dens_sweep_smem_bytes();
+  if (verlet) {
+    k_density_f32<REACH, kDensKept, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
+    k_density_f32<REACH, kDensKeptOver, MARKS><<<nblk, kRowBlock, sm, st>>>(d);
+  } else {
+    k_density_f32<REACH, kDensSweep, MARKS><<<nblk, kRowBlock, sm, st>>>(d);
+  }
+}
+
 template <bool MARKS>
 void launch_density_f32(const DevState& d, int nblk, int reach, bool verlet, cudaStream_t st) {
-  if (verlet && reach == 2)
-    k_density_f32<2, true, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
-  else if (verlet)
-    k_density_f32<1, true, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
-  else if (reach == 2)
-    k_density_f32<2, false, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
+  if (reach == 2)
+    launch_density_reach<2, MARKS>(d, nblk, verlet, st);
   else
-    k_density_f32<1, false, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
+    launch_density_reach<1, MARKS>(d, nblk, verlet, st);
 }
 
 // The reference's pair expression in FP64 (nbdf_calculator.hpp:84-132): the
