@@ -804,13 +804,22 @@ def run_engine(args, rank, world, local_rank):
         e.sync()
         t0 = time.perf_counter()
         for _ in range(k2):
+            e.step_host(pos, vel, acc)
+        t2 = time.perf_counter() - t0
+        e.sync()
+        t0 = time.perf_counter()
+        for _ in range(k2):
             e.set_dynamics(pos, vel, acc)
             e.step(1)
             e.download_dynamics(pos, vel, acc)
-        t2 = time.perf_counter() - t0
+        t3 = time.perf_counter() - t0
         e2e = {"value": n * k2 * world / dist.max(t2), "unit": "particle-steps/s",
                "h2d_bytes_per_step": 72 * n, "d2h_bytes_per_step": 72 * n, "steps": k2,
-               "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state per step"}
+               "path": "idpd_step_host per step: pinned host pos/vel/acc in, one step, the new "
+                       "pos/vel/acc out (positions copied back during the pair passes)",
+               "three_calls": {"value": n * k2 * world / dist.max(t3),
+                               "path": "idpd_set_dynamics + idpd_step(1) + idpd_download_state "
+                                       "per step"}}
 
     batched = (replicas_bench(device=local_rank, rank=rank, world=world, dist=dist)
                if not args.no_replicas else None)

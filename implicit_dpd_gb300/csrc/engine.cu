@@ -96,6 +96,9 @@ struct idpd_handle {
   // asynchronous trajectory frames (idpd_dump_xyz_async): device staging in
   // upload order, its pinned host copy, the copy stream and the writer thread
   cudaStream_t dump_st = nullptr;
+  // idpd_step_host: the copy stream of the positions and its events
+  cudaStream_t xst = nullptr;
+  cudaEvent_t x_drift = nullptr, x_done = nullptr;
   cudaEvent_t dump_ready = nullptr, dump_done = nullptr;
   unsigned char* dump_dev = nullptr;
   unsigned char* dump_host = nullptr;
@@ -684,7 +687,7 @@ void enqueue_cells(idpd_handle* h, bool drift) {
 // One MD step; `observe` adds the per-particle virial to the pair pass and
 // the observation kernels (the records are written only for replicas whose
 // step counter is due).
-void enqueue_step(idpd_handle* h, bool observe) {
+void enqueue_step(idpd_handle* h, bool observe, cudaEvent_t drift_done = nullptr) {
   const int mode = pair_mode(h);
   DevState d = h->d;  // the step writes no fine-grained side outputs
   d.dqx = d.dqy = d.dqz = nullptr;
@@ -692,6 +695,7 @@ void enqueue_step(idpd_handle* h, bool observe) {
   if (verlet) {  // cells and lists only on rebuild steps
     const int* gate = &d.vdev->rebuild;
     launch_drift_disp(d, h->nblk, h->st);
+    if (drift_done) cudaEventRecord(drift_done, h->st);  // positions final
     launch_vl_decide(d, h->st);
     launch_bin_gated(d, h->nblk, h->st);
     launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
@@ -699,6 +703,7 @@ void enqueue_step(idpd_handle* h, bool observe) {
     launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   } else {
     launch_drift_bin(d, h->nblk, true, h->st);
+    if (drift_done) cudaEventRecord(drift_done, h->st);  // positions final
     launch_scan(d, h->ncell_tot, h->R - 1, h->st);
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
@@ -875,6 +880,9 @@ int idpd_destroy(idpd_handle* h) {
   if (h->dump_ready) cudaEventDestroy(h->dump_ready);
   if (h->dump_done) cudaEventDestroy(h->dump_done);
   if (h->dump_st) cudaStreamDestroy(h->dump_st);
+  if (h->xst) cudaStreamDestroy(h->xst);
+  if (h->x_drift) cudaEventDestroy(h->x_drift);
+  if (h->x_done) cudaEventDestroy(h->x_done);
   free_all(h);
   if (h->chem) cudaFree(h->chem);
   if (h->walks) walk_destroy(h->walks);
@@ -1336,6 +1344,75 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
   CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   h->density_valid = false;
   if ((rc = sync_counts(h))) return rc;
+  return check_device_error(h);
+}
+
+// One step on host arrays: the rows in as idpd_set_dynamics, one step as
+// idpd_step(1) (the same kernels, enqueued directly so that the end of the
+// drift can be marked), the rows out as idpd_download_state. Positions are
+// final after the drift, so they are gathered and copied back on a second
+// stream while the pair passes run; velocities and accelerations follow the
+// step. One synchronisation at the end.
+int idpd_step_host(idpd_handle* h, int32_t r, double* pos, double* vel, double* acc) {
+  if (!h || r < 0 || r >= h->R || !pos || !vel || !acc)
+    return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
+  cudaSetDevice(h->device);
+  if (h->chem_on)
+    return fail(h, IDPD_ERR_STATE,
+                "the reaction can add particles during the step: use idpd_set_dynamics, "
+                "idpd_step and idpd_download_state");
+  int rc = idpd_set_dynamics(h, r, pos, vel, acc);
+  if (rc) return rc;
+  if (!h->on_device || h->layout_dirty) {  // the first step of a new layout
+    if ((rc = idpd_step(h, 1))) return rc;
+    return idpd_download_state(h, r, pos, vel, acc, nullptr, nullptr, nullptr, nullptr);
+  }
+  if (h->n_tot == 0) return IDPD_OK;
+  h->pairs_valid = true;
+  if ((rc = ensure_verlet_ready(h)) || (rc = ensure_phit(h))) return rc;
+  bool observe = false;
+  if (h->obs_period > 0) {
+    if ((rc = ensure_obs(h))) return rc;
+    std::vector<uint32_t> time(h->R);
+    CK(cudaMemcpyAsync(time.data(), h->d.rep_time, sizeof(uint32_t) * h->R, cudaMemcpyDeviceToHost,
+                       h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (uint32_t t : time) observe = observe || (t % (uint32_t)h->obs_period) == 0u;
+  }
+  if (!h->xst) {
+    CK(cudaStreamCreateWithFlags(&h->xst, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->x_drift, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->x_done, cudaEventDisableTiming));
+  }
+  const RepDev& R = h->reps_h[r];
+  const size_t n = (size_t)R.n;
+  const DevState& d = h->d;
+  CK(cudaEventRecord(h->ev0, h->st));
+  enqueue_step(h, observe, h->x_drift);
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "step launch: %s", cudaGetErrorString(le));
+  CK(cudaEventRecord(h->ev1, h->st));
+  // positions: gathered to upload order and copied back during the pair passes
+  CK(cudaStreamWaitEvent(h->xst, h->x_drift, 0));
+  struct F { const double *x, *y, *z; double* out; } f3[3] = {
+      {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
+  for (int k = 0; k < 3; k++) {
+    cudaStream_t s = k == 0 ? h->xst : h->st;
+    double* view = static_cast<double*>(const_cast<void*>(device_view(f3[k].out)));
+    double* tmp = view ? view : h->xfer + 3 * n * k;
+    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.loc, R.row_off, tmp, (int)n, s);
+    if (!view) CK(cudaMemcpyAsync(f3[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaEventRecord(h->x_done, h->xst));
+  // a reorder permutes the storage rows: not while the positions are read
+  CK(cudaStreamWaitEvent(h->st, h->x_done, 0));
+  if (++h->steps_since_sort >= h->sort_period) {
+    if ((rc = enqueue_reorder(h))) return rc;
+    h->steps_since_sort = 0;
+  }
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  h->density_valid = false;
   return check_device_error(h);
 }
 

@@ -28,7 +28,7 @@ EXPORTS = [
     "idpd_download_aux", "idpd_build_topology", "idpd_drift", "idpd_density", "idpd_force",
     "idpd_bonded", "idpd_kick", "idpd_remove_cmdrift", "idpd_step", "idpd_sync",
     "idpd_last_step_ms", "idpd_profile_step", "idpd_saru_u32", "idpd_saru_nrml_f32",
-    "idpd_cell_order", "idpd_set_dynamics", "idpd_set_tuning", "idpd_get_tuning",
+    "idpd_cell_order", "idpd_set_dynamics", "idpd_step_host", "idpd_set_tuning", "idpd_get_tuning",
     "idpd_cell_order_noalloc", "idpd_set_chem", "idpd_chem_event", "idpd_chem_get_info",
     "idpd_set_observe", "idpd_get_observations", "idpd_density_profile", "idpd_rdf",
     "idpd_dispatch_walks", "idpd_retrieve_walks", "idpd_read_run_param", "idpd_read_xyz",
@@ -86,6 +86,7 @@ def load(path=LIB_PATH):
     L.idpd_saru_nrml_f32.argtypes = [C.c_int32, U, U, U, F]
     L.idpd_cell_order.argtypes = [H, C.c_int32, VP, VP]
     L.idpd_set_dynamics.argtypes = [H, C.c_int32, VP, VP, VP]
+    L.idpd_step_host.argtypes = [H, C.c_int32, VP, VP, VP]
     L.idpd_set_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_get_tuning.argtypes = [H, C.POINTER(IdpdTuning)]
     L.idpd_list_rebuilds.argtypes = [H, C.POINTER(C.c_uint64)]
@@ -240,6 +241,11 @@ class Engine:
         """pos/vel/acc: C-contiguous float64 (n, 3) arrays (pinned for speed)."""
         self._ck(self.L.idpd_set_dynamics(self.h, replica, _p(pos), _p(vel), _p(acc)),
                  "set_dynamics")
+
+    def step_host(self, pos, vel, acc, replica=0):
+        """One step on host (n, 3) float64 arrays, updated in place
+        (idpd_step_host): set_dynamics + step(1) + download_dynamics in one call."""
+        self._ck(self.L.idpd_step_host(self.h, replica, _p(pos), _p(vel), _p(acc)), "step_host")
 
     def download_dynamics(self, pos, vel, acc, replica=0):
         """Fills caller-provided (n, 3) float64 arrays, e.g. pinned buffers."""

@@ -143,6 +143,16 @@ int idpd_set_dynamics(idpd_handle* h, int32_t replica, const double* pos, const 
  * they were uploaded (new particles from chemistry appended). */
 int idpd_download_state(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc,
                         uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit);
+/* One MD step on host arrays: the reference's loop body (src/main.cpp:166-209)
+ * with the particles' FPDPD pos/vel/acc (ptcl_class.hpp:29-31) kept in host
+ * memory by the caller. The rows of the replica go in as idpd_set_dynamics,
+ * every replica takes one step as idpd_step(h, 1), and the new pos/vel/acc
+ * come back in place, in upload order, as idpd_download_state. The result is
+ * that of the three calls bit for bit; the positions, final after the drift,
+ * are copied back while the pair passes run, and the call synchronises once.
+ * Not with the reaction enabled (IDPD_ERR_STATE: the reaction can add
+ * particles during the step). */
+int idpd_step_host(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc);
 /* Derived per-particle fields: density[3] (FPDPD::density), press[3]
  * (FPDPD::press), nei_cm_pos[2][3] (FPDPD::nei_cm_pos), delta_sumr[3]. */
 int idpd_download_aux(idpd_handle* h, int32_t replica, double* density, double* press,

@@ -1,0 +1,101 @@
+"""idpd_step_host: one step on host arrays in one call (the rows in, one step,
+the rows out, with the positions copied back while the pair passes run)
+must leave exactly the state of idpd_set_dynamics + idpd_step(1) +
+idpd_download_state, step after step: with and without kept lists, across
+list rebuilds and storage reorders, and on a batched handle."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from helpers import mdpd_params, mixed_system
+from implicit_dpd_gb300 import configs
+from implicit_dpd_gb300.abi import IdpdChemParams
+from implicit_dpd_gb300.engine import Engine, EngineError
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(p, st, n_amp, skin, sort_period):
+    e = Engine(sort_period=sort_period)
+    e.set_params(p)
+    e.upload(st)
+    e.build_topology(n_amp, [0, 3])
+    e.set_tuning(1, skin)
+    return e
+
+
+@pytest.mark.parametrize("skin,sort_period", [(0.0, 100), (0.3, 3), (0.15, 2)])
+def test_step_host_equals_the_three_calls(skin, sort_period):
+    box, st, n_amp = mixed_system(seed=21)
+    p = mdpd_params(box, time=5)
+    a = _engine(p, st, n_amp, skin, sort_period)
+    b = _engine(p, st, n_amp, skin, sort_period)
+    n = len(st["pos"])
+    pa, va, aa = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    pb, vb, ab = pa.copy(), va.copy(), aa.copy()
+    for step in range(12):
+        a.set_dynamics(pa, va, aa)
+        a.step(1)
+        a.download_dynamics(pa, va, aa)
+        b.step_host(pb, vb, ab)
+        for x, y, name in ((pa, pb, "pos"), (va, vb, "vel"), (aa, ab, "acc")):
+            assert np.array_equal(x, y), f"{name} differs at step {step}"
+    # the host copy is the device state
+    out = b.download()
+    assert np.array_equal(out["pos"], pb) and np.array_equal(out["acc"], ab)
+    assert out["pos"].shape == (n, 3)
+    if skin > 0:
+        assert b.list_rebuilds() == a.list_rebuilds() and b.list_rebuilds() > 1
+    a.close()
+    b.close()
+
+
+def test_step_host_on_a_batched_handle():
+    # replica 1 is exchanged; both replicas step
+    box = np.array([8.0, 8.0, 8.0])
+    reps = [configs.liquid(box, 3.0, seed=s) for s in (3, 4)]
+    for st in reps:
+        st["id"] = np.arange(len(st["pos"]), dtype=np.uint32)
+
+    def make():
+        e = Engine(n_replicas=2)
+        for r, st in enumerate(reps):
+            e.set_params(mdpd_params(box, seed=11 + r, time=3), replica=r)
+            e.upload(st, replica=r)
+        e.set_tuning(1, 0.2)
+        return e
+
+    a, b = make(), make()
+    st = reps[1]
+    pa, va, aa = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    pb, vb, ab = pa.copy(), va.copy(), aa.copy()
+    for _ in range(6):
+        a.set_dynamics(pa, va, aa, replica=1)
+        a.step(1)
+        a.download_dynamics(pa, va, aa, replica=1)
+        b.step_host(pb, vb, ab, replica=1)
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(aa, ab)
+    assert np.array_equal(a.download(replica=0)["pos"], b.download(replica=0)["pos"])
+    a.close()
+    b.close()
+
+
+def test_step_host_refuses_the_reaction():
+    box = np.array([10.0, 10.0, 10.0])
+    n_amp = 600
+    st = configs.flat_bilayers(box, n_amp, seed=5, jitter=0.05)
+    p = O.derive_params(configs.run_param(box))
+    p.seed, p.time = 1, 5
+    core = [int(st["id"][(st["amp_id"] == 0) & (st["unit"] == 0)][0])]
+    cp = IdpdChemParams(p_thresld=0.3, eps=0.2, influ_rad=2.0, influ_hei=0.8, influ_dep=4.0,
+                        influ_grd=-0.5, amp_num=n_amp, max_amp_num=700)
+    e = Engine()
+    e.set_params(p)
+    e.upload(st)
+    e.build_topology(n_amp, [0])
+    e.set_chem(cp, 1234, core, 64)
+    e.step(1)
+    pos, vel, acc = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    with pytest.raises(EngineError, match="reaction"):
+        e.step_host(pos, vel, acc)
+    e.close()
