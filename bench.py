@@ -535,12 +535,14 @@ def replica_observables_cpu(reps, rank, world, dist, steps=3):
 def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     """Batched MDPD replicas (256 liquids of 2k-60k particles, Warren form,
     A in [-50, -30], B = 25, densities 5-7): all of a rank's replicas in one
-    handle, one CUDA graph per step, against the same replicas stepped one
-    handle at a time with the same tuning (reach, skin and force-pass shape,
-    picked by the package's tuner on the batch). On
+    handle, the steps of a call in one graph launch (and, for comparison, one
+    graph launch per step), against the same replicas stepped one handle at
+    a time with the same tuning (reach, skin and force-pass shape, picked by
+    the package's tuner on the batch). On
     several ranks the replicas are dealt out by LPT on their particle counts
     (no exchange while stepping); the job's rate is all particles x steps
     over the slowest rank's time. Returns particle-steps/s of both forms."""
+    from implicit_dpd_gb300.abi import CFG_STEP_PER_LAUNCH
     from implicit_dpd_gb300.engine import Engine
     from implicit_dpd_gb300.partition import imbalance, lpt_partition
 
@@ -559,10 +561,35 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     # the package's tuner on the batch: (reach, skin), then the force pass's shape
     tuned, _ = autotune(eb, steps=20)
     reach, skin, lanes, blocks = tuned["reach"], tuned["skin"], tuned["lanes"], tuned["blocks"]
+    # every arm starts from this state (the batch after the tuner's ~270 steps)
+    # and takes the same 3 warm-up steps, so all arms time the same trajectory
+    start = [eb.download(replica=k) for k in range(len(mine))]
+    t_start = [eb.get_params(k).time for k in range(len(mine))]
+
+    def upload(e, k, replica):
+        q = type(params[mine[k]]).from_buffer_copy(params[mine[k]])
+        q.time = t_start[k]
+        e.set_params(q, replica)
+        s0 = start[k]
+        e.upload({key: s0[key] for key in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit")},
+                 replica)
+
+    for k in range(len(mine)):  # the same fresh start (lists built anew) as the other arms
+        upload(eb, k, k)
     eb.step(3)
     dist.barrier()
-    eb.step(steps)
+    eb.step(steps)  # the steps in one graph launch (the step in a WHILE node)
     batched = n_tot * steps / (dist.max(eb.last_step_ms()) * 1e-3)
+    # the same batch with one graph launch per step
+    ep = Engine(n_replicas=len(mine), device=device, flags=CFG_STEP_PER_LAUNCH)
+    for k in range(len(mine)):
+        upload(ep, k, k)
+    ep.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+    ep.step(3)
+    dist.barrier()
+    ep.step(steps)
+    per_step_launch = n_tot * steps / (dist.max(ep.last_step_ms()) * 1e-3)
+    ep.close()
     # what one persistent launch could save at most: the graph step's time
     # beyond its kernels' own times. Compared at skin 0, where every step does
     # the same work (cells and all passes): 20 graph steps against the mean of
@@ -576,10 +603,9 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     kernels_ms = sum(statistics.mean(p_[k] for p_ in prof) for k in prof[0])
     eb.close()
     singles = []
-    for i in mine:
+    for k in range(len(mine)):
         e = Engine(device=device)
-        e.set_params(params[i])
-        e.upload(reps[i]["state"])
+        upload(e, k, 0)
         e.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
         e.step(3)
         singles.append(e)
@@ -595,7 +621,11 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
         e.close()
     return {"workload": "mdpd_replicas_256", "n_replicas": n_rep, "n_particles": int(n_tot),
             "steps": steps, "tuning": tuned,
-            "batched": batched, "one_at_a_time": one_at_a_time,
+            "batched": batched, "batched_per_step_launch": per_step_launch,
+            "one_at_a_time": one_at_a_time,
+            "launch": "batched: the steps of one idpd_step call in one graph launch (the "
+                      "captured step repeated by a conditional WHILE node on the device); "
+                      "batched_per_step_launch: one graph launch per step",
             "speedup": batched / one_at_a_time, "unit": "particle-steps/s",
             "launch_gaps": {"tuning": {"reach": reach, "skin": 0.0}, "graph_ms_per_step": graph_ms,
                             "kernels_ms_per_step": kernels_ms,

@@ -91,6 +91,10 @@ struct idpd_handle {
   int* obs_count = nullptr;
   ObsBuffers obs_buf{};                 // per-layout scratch (null until needed)
   cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
+  // K steps in one launch: the step inside a WHILE conditional node
+  cudaGraphExec_t graph_loop = nullptr;
+  int* loop_left = nullptr;  // device count of the loop's steps left
+  bool loop_failed = false;  // the loop graph could not be built: one launch per step
   WalkState* walks = nullptr;           // FDPS multi-walk buffers (created on first use)
   unsigned long long* pair_sum = nullptr;  // device word of idpd_pair_count
   // asynchronous trajectory frames (idpd_dump_xyz_async): device staging in
@@ -143,6 +147,10 @@ int dalloc(idpd_handle* h, T** p, size_t count) {
 }
 
 void free_all(idpd_handle* h) {
+  if (h->graph_loop) {
+    cudaGraphExecDestroy(h->graph_loop);
+    h->graph_loop = nullptr;
+  }
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -167,6 +175,10 @@ void free_all(idpd_handle* h) {
 }
 
 void invalidate_graph(idpd_handle* h) {
+  if (h->graph_loop) {
+    cudaGraphExecDestroy(h->graph_loop);
+    h->graph_loop = nullptr;
+  }
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -316,6 +328,7 @@ int ensure_capacity(idpd_handle* h, int rows, int ncell, int nblk, int namp) {
   AL(d.blk_part, 3 * bc);
   AL(d.npair, cap);
   AL(h->pair_sum, 1);
+  AL(h->loop_left, 1);
   AL(d.rep_mean, 3 * h->R);
   AL(d.err, 1);
   AL(h->amp_rep, ac);
@@ -1284,6 +1297,42 @@ int idpd_remove_cmdrift(idpd_handle* h) {
   return check_device_error(h);
 }
 
+// The loop graph: a WHILE conditional node whose body is the captured step
+// followed by k_loop_tail. Returns false (and leaves no graph) where the
+// driver refuses any part of it; the steps then go one launch each.
+bool build_loop_graph(idpd_handle* h) {
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+  bool ok = false;
+  cudaGraphConditionalHandle cond;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t node;
+  if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      if (cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        enqueue_step(h, false);
+        launch_loop_tail(cond, h->loop_left, h->st);
+        const cudaError_t le = cudaGetLastError();
+        const cudaError_t ce = cudaStreamEndCapture(h->st, &body);
+        ok = le == cudaSuccess && ce == cudaSuccess &&
+             cudaGraphInstantiate(&h->graph_loop, g, 0) == cudaSuccess;
+      }
+    }
+  }
+  cudaGraphDestroy(g);
+  if (!ok) {
+    h->graph_loop = nullptr;
+    cudaGetLastError();  // the refusal is not an error of the step
+  }
+  return ok;
+}
+
 int idpd_step(idpd_handle* h, int32_t nsteps) {
   if (!h || nsteps < 0) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
   cudaSetDevice(h->device);
@@ -1317,7 +1366,25 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
+  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) && !h->chem_on &&
+                    h->obs_period == 0 && !h->loop_failed;
+  if (loop && !h->graph_loop && !build_loop_graph(h)) h->loop_failed = true;
   CK(cudaEventRecord(h->ev0, h->st));
+  if (loop && h->graph_loop) {
+    // the steps up to the next storage reorder in one launch each time
+    for (int left = nsteps; left > 0;) {
+      const int c = std::min(left, std::max(h->sort_period - h->steps_since_sort, 1));
+      launch_loop_set(h->loop_left, c, h->st);
+      CK(cudaGraphLaunch(h->graph_loop, h->st));
+      left -= c;
+      h->steps_since_sort += c;
+      if (h->steps_since_sort >= h->sort_period) {
+        if ((rc = enqueue_reorder(h))) return rc;
+        h->steps_since_sort = 0;
+      }
+    }
+    nsteps = 0;
+  }
   for (int k = 0; k < nsteps; k++) {
     bool observe = false;
     for (uint32_t& t : time) {

@@ -309,6 +309,24 @@ void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* s
   k_time_advance<<<(R + 127) / 128, 128, 0, st>>>(d.rep_time, R, skip);
 }
 
+// ------------------------------------------- K steps in one graph launch
+// The step repeated on the device by a WHILE conditional node: the count of
+// steps left is set before the launch; the last node of each step takes one
+// off and keeps the loop going while steps are left.
+__global__ void k_loop_set(int* left, int n) { *left = n; }
+
+__global__ void k_loop_tail(cudaGraphConditionalHandle cond, int* left) {
+  const int l = *left - 1;
+  *left = l;
+  cudaGraphSetConditional(cond, l > 0 ? 1u : 0u);
+}
+
+void launch_loop_set(int* left, int n, cudaStream_t st) { k_loop_set<<<1, 1, 0, st>>>(left, n); }
+
+void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, cudaStream_t st) {
+  k_loop_tail<<<1, 1, 0, st>>>(cond, left);
+}
+
 // ----------------------------------------------------------- utilities
 __global__ void k_saru_test(int n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
                             int draws, uint32_t* out_u, float* out_n) {
