@@ -1317,7 +1317,7 @@ bool build_loop_graph(idpd_handle* h) {
       if (cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0,
                                         cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
         enqueue_step(h, false);
-        launch_loop_tail(cond, h->loop_left, h->st);
+        launch_loop_tail(cond, h->loop_left, h->chem_on ? &h->chem->stopped : nullptr, h->st);
         const cudaError_t le = cudaGetLastError();
         const cudaError_t ce = cudaStreamEndCapture(h->st, &body);
         ok = le == cudaSuccess && ce == cudaSuccess &&
@@ -1366,7 +1366,7 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
-  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) && !h->chem_on &&
+  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) &&
                     h->obs_period == 0 && !h->loop_failed;
   if (loop && !h->graph_loop && !build_loop_graph(h)) h->loop_failed = true;
   CK(cudaEventRecord(h->ev0, h->st));
@@ -1378,6 +1378,15 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
       CK(cudaGraphLaunch(h->graph_loop, h->st));
       left -= c;
       h->steps_since_sort += c;
+      if (h->chem_on) {  // the loop ended early if the step's event stopped the run
+        CK(cudaMemcpyAsync(h->chem_flag_host, &h->chem->stopped, sizeof(int),
+                           cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        if (*h->chem_flag_host) {
+          h->chem_stopped = true;
+          break;
+        }
+      }
       if (h->steps_since_sort >= h->sort_period) {
         if ((rc = enqueue_reorder(h))) return rc;
         h->steps_since_sort = 0;

@@ -312,19 +312,21 @@ void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* s
 // ------------------------------------------- K steps in one graph launch
 // The step repeated on the device by a WHILE conditional node: the count of
 // steps left is set before the launch; the last node of each step takes one
-// off and keeps the loop going while steps are left.
+// off and keeps the loop going while steps are left and, with the reaction
+// enabled, while the reaction has not stopped the run (stop: its flag).
 __global__ void k_loop_set(int* left, int n) { *left = n; }
 
-__global__ void k_loop_tail(cudaGraphConditionalHandle cond, int* left) {
+__global__ void k_loop_tail(cudaGraphConditionalHandle cond, int* left, const int* stop) {
   const int l = *left - 1;
   *left = l;
-  cudaGraphSetConditional(cond, l > 0 ? 1u : 0u);
+  cudaGraphSetConditional(cond, (l > 0 && !(stop && *stop)) ? 1u : 0u);
 }
 
 void launch_loop_set(int* left, int n, cudaStream_t st) { k_loop_set<<<1, 1, 0, st>>>(left, n); }
 
-void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, cudaStream_t st) {
-  k_loop_tail<<<1, 1, 0, st>>>(cond, left);
+void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, const int* stop,
+                      cudaStream_t st) {
+  k_loop_tail<<<1, 1, 0, st>>>(cond, left, stop);
 }
 
 // ----------------------------------------------------------- utilities

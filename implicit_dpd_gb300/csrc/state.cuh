@@ -253,7 +253,8 @@ void launch_cmdrift(const DevState& d, int nblk, int R, bool force_now, cudaStre
 void launch_time_advance(const DevState& d, int R, cudaStream_t st, const int* skip = nullptr);
 // The K-step loop graph: the count of steps, and the last node of each step.
 void launch_loop_set(int* left, int n, cudaStream_t st);
-void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, cudaStream_t st);
+void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, const int* stop,
+                      cudaStream_t st);
 void launch_saru_test(int n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3, int draws,
                       uint32_t* out_u, float* out_n, cudaStream_t st);
 void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n, cudaStream_t st);

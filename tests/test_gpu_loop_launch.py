@@ -2,14 +2,16 @@
 step inside a conditional WHILE node) instead of one launch per step. The
 kernels and their order are the same, so the state after K steps must be
 the same bit for bit, with and without kept lists, across storage reorders
-that fall inside the K steps, and for batched replicas."""
+that fall inside the K steps, for batched replicas, and with the reaction
+enabled (the loop ends on the device after the step whose event stopped the
+run)."""
 import numpy as np
 import pytest
 
 from helpers import mdpd_params, mixed_system
 from implicit_dpd_gb300 import configs
 from implicit_dpd_gb300.abi import CFG_STEP_PER_LAUNCH, FORM_WARREN
-from implicit_dpd_gb300.engine import Engine, derive_params
+from implicit_dpd_gb300.engine import Engine, EngineError, derive_params
 
 pytestmark = pytest.mark.gpu
 
@@ -63,3 +65,44 @@ def test_batched_replicas_one_launch():
     a, b = run(0), run(CFG_STEP_PER_LAUNCH)
     for x, y in zip(a, b):
         assert np.array_equal(x["pos"], y["pos"]) and np.array_equal(x["vel"], y["vel"])
+
+
+def test_reaction_in_one_launch_stops_where_the_steps_do():
+    # the reaction's event runs inside the loop; the loop ends after the step
+    # whose event reached max_amp_num, as the one-launch-per-step form does
+    from implicit_dpd_gb300.abi import IdpdChemParams
+    import pyoracle as O
+
+    box = np.array([10.0, 10.0, 10.0])
+    n_amp = 600
+    st = configs.flat_bilayers(box, n_amp, seed=5, jitter=0.05)
+    core = [0, 1, 7]
+    core_ptcl = [int(st["id"][(st["amp_id"] == a) & (st["unit"] == 0)][0]) for a in core]
+
+    def run(flags):
+        p = O.derive_params(configs.run_param(box, cf_b_rigid=20.0))
+        p.seed, p.time = 1, 5
+        cp = IdpdChemParams(p_thresld=0.3, eps=0.2, influ_rad=2.0, influ_hei=0.8, influ_dep=4.0,
+                            influ_grd=-0.5, amp_num=n_amp, max_amp_num=640)
+        e = Engine(flags=flags, sort_period=4)
+        e.set_params(p)
+        e.upload(st)
+        e.build_topology(n_amp, core)
+        e.set_chem(cp, 1234, core_ptcl, 200, beg_chem=6)
+        stopped = False
+        for k in (3, 8, 8, 8, 8):
+            try:
+                e.step(k)
+            except EngineError:
+                stopped = True
+                break
+        out = e.download()
+        t = e.get_params().time
+        e.close()
+        return out, t, stopped
+
+    (a, ta, sa), (b, tb, sb) = run(0), run(CFG_STEP_PER_LAUNCH)
+    assert sa == sb and ta == tb
+    assert len(a["pos"]) == len(b["pos"]) > len(st["pos"])
+    for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit"):
+        assert np.array_equal(a[k], b[k]), k
