@@ -1366,42 +1366,36 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
-  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) &&
-                    h->obs_period == 0 && !h->loop_failed;
+  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) && !h->loop_failed;
   if (loop && !h->graph_loop && !build_loop_graph(h)) h->loop_failed = true;
+  const bool use_loop = loop && h->graph_loop;
+  // whether the step `ahead` steps from now observes: some replica's step
+  // counter is then a multiple of the period
+  auto observes = [&](int ahead) {
+    for (uint32_t t : time)
+      if (((t + (uint32_t)ahead) % (uint32_t)h->obs_period) == 0u) return true;
+    return false;
+  };
   CK(cudaEventRecord(h->ev0, h->st));
-  if (loop && h->graph_loop) {
-    // the steps up to the next storage reorder in one launch each time
-    for (int left = nsteps; left > 0;) {
-      const int c = std::min(left, std::max(h->sort_period - h->steps_since_sort, 1));
+  for (int k = 0; k < nsteps;) {
+    // an observing step is one launch of the observation graph; a run of
+    // other steps up to the next storage reorder is one launch of the loop
+    const bool obs = !time.empty() && observes(0);
+    int c = 1;
+    if (!obs && use_loop) {
+      const int room = std::max(h->sort_period - h->steps_since_sort, 1);
+      while (k + c < nsteps && c < room && !(!time.empty() && observes(c))) c++;
+    }
+    if (c > 1) {
       launch_loop_set(h->loop_left, c, h->st);
       CK(cudaGraphLaunch(h->graph_loop, h->st));
-      left -= c;
-      h->steps_since_sort += c;
-      if (h->chem_on) {  // the loop ended early if the step's event stopped the run
-        CK(cudaMemcpyAsync(h->chem_flag_host, &h->chem->stopped, sizeof(int),
-                           cudaMemcpyDeviceToHost, h->st));
-        CK(cudaStreamSynchronize(h->st));
-        if (*h->chem_flag_host) {
-          h->chem_stopped = true;
-          break;
-        }
-      }
-      if (h->steps_since_sort >= h->sort_period) {
-        if ((rc = enqueue_reorder(h))) return rc;
-        h->steps_since_sort = 0;
-      }
+    } else {
+      CK(cudaGraphLaunch(obs ? h->graph_obs : h->graph, h->st));
     }
-    nsteps = 0;
-  }
-  for (int k = 0; k < nsteps; k++) {
-    bool observe = false;
-    for (uint32_t& t : time) {
-      observe = observe || (t % (uint32_t)h->obs_period) == 0u;
-      t++;
-    }
-    CK(cudaGraphLaunch(observe ? h->graph_obs : h->graph, h->st));
-    if (++h->steps_since_sort >= h->sort_period) {
+    for (uint32_t& t : time) t += (uint32_t)c;
+    k += c;
+    h->steps_since_sort += c;
+    if (h->steps_since_sort >= h->sort_period) {
       if ((rc = enqueue_reorder(h))) return rc;
       h->steps_since_sort = 0;
     }

@@ -113,8 +113,8 @@ typedef struct idpd_config {
 #define IDPD_CFG_FP64_KEPT 0x4
 /* idpd_step(h, K) launches one graph per step. By default the K steps go to
  * the device in one launch: a graph whose conditional WHILE node repeats the
- * captured step K times (between storage reorders; one launch per step with
- * observations enabled). Results are the same either way. */
+ * captured step K times (between storage reorders and observing steps).
+ * Results are the same either way. */
 #define IDPD_CFG_STEP_PER_LAUNCH 0x8
 
 int idpd_create(const idpd_config* cfg, idpd_handle** out);
@@ -192,10 +192,10 @@ int idpd_remove_cmdrift(idpd_handle* h);
 /* nsteps iterations of the main loop body of src/main.cpp:166-184 (drift,
  * density, force, bonded, kick, centre-of-mass drift removal every 100 steps,
  * time += 1) for every replica, captured once into a CUDA graph. The steps up
- * to the next storage reorder go to the device in one launch (the graph's
- * conditional WHILE node repeats the step, and ends the loop after a step
- * whose reaction event stopped the run); with observations enabled, or with
- * IDPD_CFG_STEP_PER_LAUNCH, each step is one launch.
+ * to the next storage reorder or observing step go to the device in one
+ * launch (the graph's conditional WHILE node repeats the step, and ends the
+ * loop after a step whose reaction event stopped the run); an observing step
+ * is one launch, and with IDPD_CFG_STEP_PER_LAUNCH every step is.
  * Per-particle press and nei_cm_pos are not produced by this path. */
 int idpd_step(idpd_handle* h, int32_t nsteps);
 /* Blocks until the handle's stream is idle; reports device-side errors. */

@@ -106,3 +106,32 @@ def test_reaction_in_one_launch_stops_where_the_steps_do():
     assert len(a["pos"]) == len(b["pos"]) > len(st["pos"])
     for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_observing_steps_between_loop_launches():
+    # with observations every 4 steps, the steps between them go in loop
+    # launches and each observing step in the observation graph: the records
+    # and the state equal those of one launch per step
+    def run(flags):
+        box, st, n_amp = mixed_system(seed=41)
+        e = Engine(flags=flags, sort_period=6)
+        e.set_params(mdpd_params(box, time=2))
+        e.upload(st)
+        e.build_topology(n_amp, [0, 3])
+        e.set_tuning(1, 0.2)
+        e.set_observe(4)
+        for k in (5, 11, 1, 9):
+            e.step(k)
+        obs = e.observations()
+        out = e.download()
+        e.close()
+        return obs, out
+
+    (oa, a), (ob, b) = run(0), run(CFG_STEP_PER_LAUNCH)
+    assert len(oa) == len(ob) > 0
+    assert [o["time"] for o in oa] == [o["time"] for o in ob]
+    for x, y in zip(oa, ob):
+        for k in x:
+            assert np.array_equal(np.asarray(x[k]), np.asarray(y[k])), k
+    for k in ("pos", "vel", "acc"):
+        assert np.array_equal(a[k], b[k]), k
