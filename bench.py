@@ -880,8 +880,11 @@ def run_engine(args, rank, world, local_rank):
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "fp64_same_algorithm": fp64_same,
            "e2e": e2e, "cpu_baseline": cpu,
            "batched_replicas": batched, "reaction": reaction, "liquid": liquid,
-           "gpu_launches": args.steps * (KERNELS_PER_KEPT_STEP if reach["skin"] > 0 else KERNELS_PER_STEP)
-                           + n_reorders * KERNELS_PER_REORDER,
+           # per step its kernels and the loop's tail node; per launch of the
+           # loop its count kernel (one launch, split at each reorder)
+           "gpu_launches": args.steps * ((KERNELS_PER_KEPT_STEP if reach["skin"] > 0
+                                          else KERNELS_PER_STEP) + 1)
+                           + (n_reorders + 1) + n_reorders * KERNELS_PER_REORDER,
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
     if rank == 0:
         print(json.dumps(out), flush=True)
