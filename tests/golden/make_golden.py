@@ -50,7 +50,7 @@ influ_grd -0.5
 core_amp_id 0
 """
 
-# run_param sets: the survey container defaults (input_generator.py:20-43),
+# run_param sets: the reference input generator's defaults (input_generator.py:20-43),
 # the MPI test set (test/mpi_bonded/result_mpi/31x31/run_param.txt), and one
 # with negative off-diagonal cf_r (harmonic-mean gamma, parameter.hpp:139-144).
 PARAM_SETS = [

@@ -5,9 +5,9 @@ import pyoracle as O
 from implicit_dpd_gb300 import configs
 from implicit_dpd_gb300.abi import FORM_MDPD, FORM_PAIRWISE, FORM_WARREN
 
-# Relative force bar of the benchmark spec: ||F_gpu - F_ref|| / max(||F_ref||, F_floor)
+# Relative force bar of the engine: ||F_gpu - F_ref|| / max(||F_ref||, F_floor)
 # <= 1e-5 for every particle, with F_floor the RMS of ||F_ref|| over the
-# system (a particle whose forces happen to cancel is judged against the
+# system (a particle whose forces happen to cancel is measured against the
 # typical force scale, not against its own near-zero magnitude).
 FORCE_TOL = 1.0e-5
 
