@@ -737,6 +737,26 @@ def pair_roofline(kernel_ms, pairs, n, clocks, device, which=None):
                                                  if traffic else None)}}
 
 
+def step_roofline(roofline, n, ms_per_step):
+    """The step against the sum of its passes' lower-bound times: the two pair
+    passes at the issue bound (their algorithmic lane operations per ordered
+    pair x the counted pairs over the peak issue rate), the rest of the step
+    at the measured copy bandwidth (176 compulsory HBM bytes per
+    particle-step)."""
+    pairs, peak = roofline["ordered_pairs"], roofline["peak"] * 1e12
+    hbm_peak, _ = measured_peaks()
+    parts = {"force_ms": OPS_PER_ORDERED_PAIR["force"] * pairs / peak * 1e3,
+             "density_ms": OPS_PER_ORDERED_PAIR["density"] * pairs / peak * 1e3,
+             "hbm_ms": STEP_BYTES_PER_PARTICLE * n / (hbm_peak * 1e9) * 1e3}
+    lower = sum(parts.values())
+    return {"lower_bound_ms": lower, "ms_per_step": ms_per_step, "frac": lower / ms_per_step,
+            "parts": parts,
+            "definition": "sum of the passes' lower-bound times (pair passes at 4 issue slots x "
+                          "32 lanes x SMs x clock for their algorithmic lane operations, the "
+                          "rest at the measured copy bandwidth for 176 B per particle-step) "
+                          "over the measured step"}
+
+
 def fp64_arms(st64, n_amp, rp, tune, value32, steps, device):
     """Both FP64 arms on one state: particle-steps/s, the FP32 engine's
     speed-up over each, and the FP32 engine's pair-force error against each
@@ -884,6 +904,7 @@ def run_engine(args, rank, world, local_rank):
                                                pairs_per_bead=pairs / n,
                                                parallelism=f"replicas{world}" if world > 1 else "single"),
            "clocks": clocks, "roofline": roofline, "step_hbm_gbs": step_gbs,
+           "step_roofline": step_roofline(roofline, n, ms_max / args.steps),
            "kernel_ms": kernel_ms, "fp64_plain": fp64, "fp64_same_algorithm": fp64_same,
            "e2e": e2e, "cpu_baseline": cpu,
            "batched_replicas": batched, "reaction": reaction, "liquid": liquid,
