@@ -120,7 +120,7 @@ struct ChemDev {
 
 constexpr int kRowBlock = 128;  // rows per block of row-block launches
 constexpr int kNbrCap = 512;    // neighbour-list slots per particle
-constexpr int kVerletCap = 1024; // kept-list slots per particle
+constexpr int kVerletCap = 512;  // kept-list slots per particle
 
 // kernels_cells.cu
 void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t st);

@@ -129,7 +129,7 @@ def test_kept_list_pair_forces_at_fp64_accuracy():
 
 
 def test_list_overflows_match_oracle():
-    """rho 400: the pass-1 lists (512) and the kept lists (1,024) overflow,
+    """rho 400: the pass-1 lists (512) and the kept lists (512) overflow,
     so both FP64 passes sweep the 27 cells with the ownership rule."""
     box = np.array([5.0, 5.0, 5.0])
     rng = np.random.default_rng(40)
