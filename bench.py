@@ -426,7 +426,7 @@ def reaction_bench(tune, steps=100, equil=2000, device=0):
 def liquid_bench(steps=200, equil=300, device=0):
     """The 10^6-particle MDPD liquid: 55^3 box at density 6 (998,250
     particles), Warren form A = -40, B = 25, r_d = 0.75, sigma 3, dt 0.005,
-    uniform random start. The FP32 engine (tuned over reach and skin) against
+    uniform random start. The FP32 engine (tuned by the package's tuner) against
     the plain FP64 kernels of the same step, with the measured force error."""
     from implicit_dpd_gb300.abi import CFG_FP64_KEPT, CFG_FP64_PAIRS, FORM_WARREN
     from implicit_dpd_gb300.engine import Engine, derive_params
@@ -446,14 +446,9 @@ def liquid_bench(steps=200, equil=300, device=0):
 
     e = engine()
     e.step(equil)
-    times = {}
-    for reach, skin in [(1, 0.0), (1, 0.15), (1, 0.2), (1, 0.3)]:
-        e.set_tuning(reach, skin)
-        e.step(2)
-        e.step(30)
-        times[(reach, skin)] = e.last_step_ms() / 30
-    reach, skin = min(times, key=times.get)
-    e.set_tuning(reach, skin)
+    # the package's tuner: (reach, skin), then the force pass's launch shape
+    tuned, _ = autotune(e)
+    reach, skin = tuned["reach"], tuned["skin"]
     e.step(3)
     e.step(steps)
     v32 = n * steps / (e.last_step_ms() * 1e-3)
@@ -485,7 +480,7 @@ def liquid_bench(steps=200, equil=300, device=0):
     vk = n * 10 / (ek.last_step_ms() * 1e-3)
     ek.close()
     return {"workload": "mdpd_liquid_1m", "n_particles": int(n), "steps": steps,
-            "equilibration_steps": equil, "tuning": {"reach": reach, "skin": skin},
+            "equilibration_steps": equil, "tuning": tuned,
             "value": v32, "fp64_plain": v64, "speedup_fp32_over_fp64": v32 / v64,
             "fp64_same_algorithm": vk, "speedup_fp32_over_fp64_same_algorithm": v32 / vk,
             "force_error_vs_fp64_same_algorithm": float(errk.max()),
