@@ -54,13 +54,19 @@ STEP_BYTES_PER_PARTICLE = 176  # compulsory HBM bytes of one particle-step
 # (the Saru hash and draws) + 5 SFU (sqrt r, rcp, sqrt w, log, cos); the
 # density pass ~12 FP32 + 1 SFU.
 OPS_PER_ORDERED_PAIR = {"force": 134, "density": 13}
-KERNELS_PER_STEP = 16          # drift_bin, scan x3, scatter, cell_sort, pack, density,
-                               # density finalize, force, force walk, bonded_kick,
-                               # cmdrift x3, time
-KERNELS_PER_KEPT_STEP = 20     # drift_disp, rebuild decision, gated bin, gated scan x3,
-                               # gated scatter / cell_sort / pack, gated list build,
-                               # density (kept lists, overflowed kept lists), density
-                               # finalize, force, force walk, bonded_kick, cmdrift x3, time
+# Kernels a captured step launches (the loop node repeats them): without kept
+# lists drift_bin, scan x3, scatter, cell_sort, pack, density, density
+# finalize, force, force walk, bonded_kick, the drift-removal condition, time,
+# the loop's tail; with kept lists drift_disp, rebuild decision, two rebuild
+# conditions, pack, density (kept lists, overflowed kept lists), density
+# finalize, force, force walk, bonded_kick, the drift-removal condition, time,
+# the loop's tail. A rebuild step adds the IF body of the cells and lists (bin,
+# scan x3, scatter, cell_sort, list build); a step whose replica counter is a
+# multiple of 100 adds the drift removal (3 kernels).
+KERNELS_PER_STEP = 15
+KERNELS_PER_KEPT_STEP = 14
+KERNELS_PER_REBUILD = 7
+KERNELS_PER_CM = 3
 KERNELS_PER_REORDER = 4        # gather, topology, identity, loc
 
 
@@ -732,6 +738,17 @@ def pair_roofline(kernel_ms, pairs, n, clocks, device, which=None):
                                                  if traffic else None)}}
 
 
+def gpu_launches(steps, kept, rebuilds, t0, n_reorders):
+    """The kernels the timed steps launch: per step those of the captured
+    step, the IF bodies that ran (rebuilds with kept lists, the drift removal
+    at step counters that are multiples of 100), one count kernel per launch
+    of the loop (split at each storage reorder) and the reorders' kernels."""
+    cm = sum(1 for t in range(t0, t0 + steps) if t % 100 == 0)
+    per = KERNELS_PER_KEPT_STEP if kept else KERNELS_PER_STEP
+    return (steps * per + (rebuilds * KERNELS_PER_REBUILD if kept else 0) + cm * KERNELS_PER_CM
+            + (n_reorders + 1) + n_reorders * KERNELS_PER_REORDER)
+
+
 def step_roofline(roofline, n, ms_per_step):
     """The step against the sum of its passes' lower-bound times: the two pair
     passes at the issue bound (their algorithmic lane operations per ordered
@@ -818,6 +835,7 @@ def run_engine(args, rank, world, local_rank):
     dist.barrier()
     e.sync()
     rb0 = e.list_rebuilds()
+    t0_step = e.get_params().time  # the step counter at the first timed step
     clk = Clocks(local_rank)
     clk.start()
     e.step(args.steps)  # CUDA events around the steps on the engine's stream
@@ -905,9 +923,8 @@ def run_engine(args, rank, world, local_rank):
            "batched_replicas": batched, "reaction": reaction, "liquid": liquid,
            # per step its kernels and the loop's tail node; per launch of the
            # loop its count kernel (one launch, split at each reorder)
-           "gpu_launches": args.steps * ((KERNELS_PER_KEPT_STEP if reach["skin"] > 0
-                                          else KERNELS_PER_STEP) + 1)
-                           + (n_reorders + 1) + n_reorders * KERNELS_PER_REORDER,
+           "gpu_launches": gpu_launches(args.steps, reach["skin"] > 0, rebuilds, t0_step,
+                                        n_reorders),
            "force_error_bar": "max-particle relative force error <= 1e-5 vs FP64 (tests/test_gpu_parity.py)"}
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -93,6 +93,7 @@ struct idpd_handle {
   cudaGraphExec_t graph_obs = nullptr;  // the step with the observation
   // K steps in one launch: the step inside a WHILE conditional node
   cudaGraphExec_t graph_loop = nullptr;
+  cudaStream_t cst = nullptr;  // captures the bodies of the step's IF nodes
   int* loop_left = nullptr;  // device count of the loop's steps left
   bool loop_failed = false;  // the loop graph could not be built: one launch per step
   WalkState* walks = nullptr;           // FDPS multi-walk buffers (created on first use)
@@ -697,6 +698,52 @@ void enqueue_cells(idpd_handle* h, bool drift) {
   launch_scatter_sort_pack(h->d, h->nblk, h->ncell_tot, true, h->st);
 }
 
+// Work that most steps skip goes, in a captured step, into the body of an IF
+// node: begin_if adds the node after the kernel that sets its condition
+// (cond launches it) and starts capturing the body on h->cst; the caller
+// enqueues the work on the returned stream; end_if ends the body. When the
+// stream is not capturing (a step enqueued directly), the work goes to h->st
+// and its kernels skip themselves, as they do inside the body too.
+struct IfScope {
+  cudaStream_t st;
+  bool body;
+};
+template <class Cond>
+IfScope begin_if(idpd_handle* h, Cond&& cond) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return {h->st, false};
+  cudaGraphConditionalHandle ch;
+  if (cudaGraphConditionalHandleCreate(&ch, g, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+    return {h->st, false};
+  cond(ch);
+  if (cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd) != cudaSuccess)
+    return {h->st, false};
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = ch;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, edges, nd, &cp) != cudaSuccess) return {h->st, false};
+  cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (cudaStreamBeginCaptureToGraph(h->cst, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return {h->st, false};  // an empty body: the kernels follow on h->st
+  return {h->cst, true};
+}
+
+void end_if(idpd_handle* h, const IfScope& s) {
+  if (!s.body) return;
+  cudaGraph_t body;
+  cudaStreamEndCapture(h->cst, &body);
+}
+
 // One MD step; `observe` adds the per-particle virial to the pair pass and
 // the observation kernels (the records are written only for replicas whose
 // step counter is due).
@@ -710,10 +757,16 @@ void enqueue_step(idpd_handle* h, bool observe, cudaEvent_t drift_done = nullptr
     launch_drift_disp(d, h->nblk, h->st);
     if (drift_done) cudaEventRecord(drift_done, h->st);  // positions final
     launch_vl_decide(d, h->st);
-    launch_bin_gated(d, h->nblk, h->st);
-    launch_scan(d, h->ncell_tot, h->R - 1, h->st, gate);
-    launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st, gate);
-    launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
+    const auto rebuild = [&](cudaGraphConditionalHandle c) { launch_cond_flag(c, gate, h->st); };
+    IfScope c = begin_if(h, rebuild);
+    launch_bin_gated(d, h->nblk, c.st);
+    launch_scan(d, h->ncell_tot, h->R - 1, c.st, gate);
+    launch_scatter_sort(d, h->nblk, h->ncell_tot, true, c.st, gate);
+    end_if(h, c);
+    launch_pack(d, h->nblk, h->st, gate);  // every step: the positions changed
+    c = begin_if(h, rebuild);
+    launch_verlet_build(d, h->nblk, h->tune.reach, c.st);
+    end_if(h, c);
   } else {
     launch_drift_bin(d, h->nblk, true, h->st);
     if (drift_done) cudaEventRecord(drift_done, h->st);  // positions final
@@ -729,7 +782,13 @@ void enqueue_step(idpd_handle* h, bool observe, cudaEvent_t drift_done = nullptr
   }
   launch_bonded_kick(d, h->nblk, true, h->st);
   if (observe) launch_observe_bonds(d, h->obs_buf, h->n_amp_tot, h->amp_rep, h->st);
-  launch_cmdrift(d, h->nblk, h->R, false, h->st);
+  {
+    IfScope c = begin_if(h, [&](cudaGraphConditionalHandle ch) {
+      launch_cond_cm(ch, d.rep_time, h->R, h->st);
+    });
+    launch_cmdrift(d, h->nblk, h->R, false, c.st);
+    end_if(h, c);
+  }
   if (h->chem_on)
     launch_chem(d, h->chem_buf, h->reps_h[0].nblk, h->chem_cfg.n_core, h->chem_amp_cap, false,
                 h->st);
@@ -875,7 +934,8 @@ int idpd_create(const idpd_config* cfg, idpd_handle** out) {
   h->n_amp.assign(h->R, 0);
   if (cudaSetDevice(h->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return fail(nullptr, IDPD_ERR_CUDA, "stream / event creation failed");
   }
@@ -894,6 +954,7 @@ int idpd_destroy(idpd_handle* h) {
   if (h->dump_done) cudaEventDestroy(h->dump_done);
   if (h->dump_st) cudaStreamDestroy(h->dump_st);
   if (h->xst) cudaStreamDestroy(h->xst);
+  if (h->cst) cudaStreamDestroy(h->cst);
   if (h->x_drift) cudaEventDestroy(h->x_drift);
   if (h->x_done) cudaEventDestroy(h->x_done);
   free_all(h);

@@ -403,14 +403,23 @@ void launch_drift_bin(const DevState& d, int nblk, bool do_drift, cudaStream_t s
   k_drift_bin<<<nblk, kRowBlock, 0, st>>>(d, do_drift ? 1 : 0);
 }
 
-void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
-                              cudaStream_t st, const int* gate) {
+void launch_scatter_sort(const DevState& d, int nblk, int ncell_tot, bool stable, cudaStream_t st,
+                         const int* gate) {
   if (nblk == 0) return;
   k_scatter<<<nblk, kRowBlock, 0, st>>>(d, gate);
   if (stable)
     k_cell_sort<<<std::min((ncell_tot + kSortWarps - 1) / kSortWarps, kSortBlocks),
                   32 * kSortWarps, 0, st>>>(d.perm, d.cell_start, ncell_tot, gate);
-  k_pack<<<nblk, kRowBlock, 0, st>>>(d, gate);
+}
+
+void launch_pack(const DevState& d, int nblk, cudaStream_t st, const int* gate) {
+  if (nblk > 0) k_pack<<<nblk, kRowBlock, 0, st>>>(d, gate);
+}
+
+void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
+                              cudaStream_t st, const int* gate) {
+  launch_scatter_sort(d, nblk, ncell_tot, stable, st, gate);
+  launch_pack(d, nblk, st, gate);
 }
 
 // ------------------------------------------------------------- reorder

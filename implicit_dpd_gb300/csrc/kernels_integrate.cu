@@ -324,6 +324,30 @@ __global__ void k_loop_tail(cudaGraphConditionalHandle cond, int* left, const in
 
 void launch_loop_set(int* left, int n, cudaStream_t st) { k_loop_set<<<1, 1, 0, st>>>(left, n); }
 
+// IF nodes of a captured step: work that most steps skip (the cell and list
+// rebuild, the centre-of-mass drift removal every kCmCorr steps) sits in a
+// conditional body whose condition one thread sets from the device state,
+// so that a step without it launches none of its kernels.
+__global__ void k_cond_flag(cudaGraphConditionalHandle cond, const int* flag) {
+  cudaGraphSetConditional(cond, *flag ? 1u : 0u);
+}
+
+__global__ void k_cond_cm(cudaGraphConditionalHandle cond, const uint32_t* rep_time, int R) {
+  int any = 0;
+  for (int r = threadIdx.x; r < R; r += blockDim.x) any |= (rep_time[r] % kCmCorr) == 0u;
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
+}
+
+void launch_cond_flag(cudaGraphConditionalHandle cond, const int* flag, cudaStream_t st) {
+  k_cond_flag<<<1, 1, 0, st>>>(cond, flag);
+}
+
+void launch_cond_cm(cudaGraphConditionalHandle cond, const uint32_t* rep_time, int R,
+                    cudaStream_t st) {
+  k_cond_cm<<<1, 256, 0, st>>>(cond, rep_time, R);
+}
+
 void launch_loop_tail(cudaGraphConditionalHandle cond, int* left, const int* stop,
                       cudaStream_t st) {
   k_loop_tail<<<1, 1, 0, st>>>(cond, left, stop);

@@ -137,6 +137,16 @@ void launch_bin_gated(const DevState& d, int nblk, cudaStream_t st);
 // keeps each slot's cell of the last rebuild.
 void launch_scatter_sort_pack(const DevState& d, int nblk, int ncell_tot, bool stable,
                               cudaStream_t st, const int* gate = nullptr);
+// The two halves of launch_scatter_sort_pack: rows to sorted slots and the
+// stable order within cells; the FP32 copies of the pair passes.
+void launch_scatter_sort(const DevState& d, int nblk, int ncell_tot, bool stable, cudaStream_t st,
+                         const int* gate = nullptr);
+void launch_pack(const DevState& d, int nblk, cudaStream_t st, const int* gate = nullptr);
+// Conditions of the IF nodes of a captured step: the rebuild flag, and
+// whether the centre-of-mass drift removal is due for some replica.
+void launch_cond_flag(cudaGraphConditionalHandle cond, const int* flag, cudaStream_t st);
+void launch_cond_cm(cudaGraphConditionalHandle cond, const uint32_t* rep_time, int R,
+                    cudaStream_t st);
 void launch_reorder(const DevState& d, const DevState& o, int nblk, int n_topol,
                     cudaStream_t st);
 void launch_update_loc(const DevState& d, int nblk, cudaStream_t st);
