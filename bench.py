@@ -410,7 +410,8 @@ def reaction_bench(tune, steps=100, equil=2000, device=0):
     n = len(both["pos"])
     both["id"] = np.arange(n, dtype=np.uint32)
     e = make_engine(both, n_amp, rp, device=device)
-    e.set_tuning(tune["reach"], tune["skin"], lanes=tune.get("lanes"), blocks=tune.get("blocks"))
+    e.set_tuning(tune["reach"], tune["skin"], lanes=tune.get("lanes"), blocks=tune.get("blocks"),
+                 dens_lanes=tune.get("dens_lanes"))
     e.step(equil)
     e.set_precursor(SOLVENT, HYPHOB, HYPHIL, precursor_threshold(1e-4), 2024)
     e.step(3)
@@ -569,6 +570,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     # the package's tuner on the batch: (reach, skin), then the force pass's shape
     tuned, _ = autotune(eb, steps=20)
     reach, skin, lanes, blocks = tuned["reach"], tuned["skin"], tuned["lanes"], tuned["blocks"]
+    dlanes = tuned["dens_lanes"]
     # every arm starts from this state (the batch after the tuner's ~270 steps)
     # and takes the same 3 warm-up steps, so all arms time the same trajectory
     start = [eb.download(replica=k) for k in range(len(mine))]
@@ -592,7 +594,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     ep = Engine(n_replicas=len(mine), device=device, flags=CFG_STEP_PER_LAUNCH)
     for k in range(len(mine)):
         upload(ep, k, k)
-    ep.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+    ep.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dlanes)
     ep.step(3)
     dist.barrier()
     ep.step(steps)
@@ -614,7 +616,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     for k in range(len(mine)):
         e = Engine(device=device)
         upload(e, k, 0)
-        e.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+        e.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dlanes)
         e.step(3)
         singles.append(e)
     import torch

@@ -151,7 +151,8 @@ class IdpdConfig(C.Structure):
 
 class IdpdTuning(C.Structure):
     _fields_ = [("reach", C.c_int32), ("skin", C.c_float), ("pair_lanes", C.c_int32),
-                ("pair_blocks", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("pair_blocks", C.c_int32), ("density_lanes", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 class IdpdPrecursor(C.Structure):

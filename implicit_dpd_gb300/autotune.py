@@ -1,7 +1,8 @@
 """The engine's autotuner: picks the cell reach and the neighbour-list skin of
 a handle, then the launch shape of the force pass (lanes per particle and
-128-row blocks per CTA), by timing each choice on the handle's current state,
-and caches the choice per GPU model and workload signature in a JSON file.
+128-row blocks per CTA), then the lanes per particle of the density pass over
+the kept lists, by timing each choice on the handle's current state, and
+caches the choice per GPU model and workload signature in a JSON file.
 
 No choice changes the pair sets (they are exact), and the fixed-point sums
 make the reach and the launch shape irrelevant to the results; a skin changes
@@ -16,6 +17,8 @@ DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15),
                    (2, 0.3))
 # (lanes per particle, row blocks per CTA) of the force pass; the first is the default
 SHAPES = ((16, 1), (8, 1), (32, 1), (8, 2), (16, 2))
+# lanes per particle of the density pass over kept lists; the first is the default
+DENS_LANES = (32, 16, 8)
 
 
 def default_cache_path():
@@ -53,21 +56,24 @@ def _store(path, table):
 
 
 def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, refresh=False,
-         shapes=SHAPES):
+         shapes=SHAPES, dens_lanes=DENS_LANES):
     """Applies the fastest (reach, skin), then the fastest force-pass shape
-    (lanes, blocks) at that (reach, skin), to `engine` and returns (choice,
-    times): choice = {"reach", "skin", "lanes", "blocks"}, times maps
-    "reach{r}_skin{s}" and "lanes{l}_blocks{b}" to ms per step (empty when the
-    choice came from the cache). With a key and a cache path, a cached choice
-    is applied without timing unless refresh is set, and a new choice is
-    written back. Choices whose skin the box does not allow are skipped."""
+    (lanes, blocks) at that (reach, skin), then the fastest density-pass lanes
+    (with kept lists), to `engine` and returns (choice, times): choice =
+    {"reach", "skin", "lanes", "blocks", "dens_lanes"}, times maps
+    "reach{r}_skin{s}", "lanes{l}_blocks{b}" and "dens_lanes{l}" to ms per
+    step (empty when the choice came from the cache). With a key and a cache
+    path, a cached choice is applied without timing unless refresh is set,
+    and a new choice is written back. Choices whose skin the box does not
+    allow are skipped."""
     table = _load(cache_path) if (cache_path and key) else {}
     if key and not refresh and key in table:
         c = table[key]
         choice = {"reach": c["reach"], "skin": c["skin"], "lanes": c.get("lanes", shapes[0][0]),
-                  "blocks": c.get("blocks", shapes[0][1])}
+                  "blocks": c.get("blocks", shapes[0][1]),
+                  "dens_lanes": c.get("dens_lanes", dens_lanes[0])}
         engine.set_tuning(choice["reach"], choice["skin"], lanes=choice["lanes"],
-                          blocks=choice["blocks"])
+                          blocks=choice["blocks"], dens_lanes=choice["dens_lanes"])
         return choice, {}
 
     def timed():
@@ -76,10 +82,11 @@ def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, r
         return engine.last_step_ms() / steps
 
     lanes0, blocks0 = shapes[0]
+    dl0 = dens_lanes[0]
     times = {}
     for reach, skin in choices:
         try:
-            engine.set_tuning(reach, skin, lanes=lanes0, blocks=blocks0)
+            engine.set_tuning(reach, skin, lanes=lanes0, blocks=blocks0, dens_lanes=dl0)
         except Exception:  # the box is too small for this skin
             continue
         times[(reach, skin)] = timed()
@@ -88,14 +95,21 @@ def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, r
     reach, skin = min(times, key=times.get)
     shape_times = {shapes[0]: times[(reach, skin)]}
     for lanes, blocks in shapes[1:]:
-        engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
+        engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl0)
         shape_times[(lanes, blocks)] = timed()
     lanes, blocks = min(shape_times, key=shape_times.get)
-    engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks)
-    choice = {"reach": reach, "skin": skin, "lanes": lanes, "blocks": blocks}
+    dens_times = {dl0: shape_times[(lanes, blocks)]}
+    if skin > 0:  # the density pass's lanes act on the kept lists only
+        for dl in dens_lanes[1:]:
+            engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
+            dens_times[dl] = timed()
+    dl = min(dens_times, key=dens_times.get)
+    engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
+    choice = {"reach": reach, "skin": skin, "lanes": lanes, "blocks": blocks, "dens_lanes": dl}
     if cache_path and key:
-        table[key] = dict(choice, ms_per_step=shape_times[(lanes, blocks)])
+        table[key] = dict(choice, ms_per_step=dens_times[dl])
         _store(cache_path, table)
     out = {f"reach{r}_skin{s:g}": t for (r, s), t in times.items()}
     out.update({f"lanes{l}_blocks{b}": t for (l, b), t in shape_times.items()})
+    out.update({f"dens_lanes{l}": t for l, t in dens_times.items()})
     return choice, out

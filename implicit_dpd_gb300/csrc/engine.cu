@@ -69,7 +69,7 @@ struct idpd_handle {
   cudaGraphExec_t graph = nullptr;
   int steps_since_sort = 0;
   float last_ms = 0.f;
-  PairTuning tune{1, 0.0f, 16, 1};
+  PairTuning tune{1, 0.0f, 16, 1, 32};
   bool vl_dirty = true;                 // cells rebuilt outside the step: the kept lists are stale
   std::string err;
   // chemistry (replica 0 of a one-replica handle)
@@ -774,7 +774,7 @@ void enqueue_step(idpd_handle* h, bool observe, cudaEvent_t drift_done = nullptr
     launch_scatter_sort_pack(d, h->nblk, h->ncell_tot, true, h->st);
   }
   const bool marks = mode == kPairsF32 && h->prec_any && d.phit;
-  launch_density(d, h->nblk, mode, h->tune.reach, verlet, marks, h->cap, h->st);
+  launch_density(d, h->nblk, mode, h->tune.reach, verlet, marks, h->cap, h->st, h->tune.dlanes);
   launch_force(d, h->nblk, mode, observe, verlet, h->tune, form_mask(h), h->cap, h->st);
   if (h->prec_any) {
     d.prec_count = h->prec_dev;
@@ -1563,6 +1563,9 @@ int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
     return fail(h, IDPD_ERR_INVALID_ARG, "pair_lanes must be 8, 16 or 32 (0: 16)");
   if (t->pair_blocks != 0 && t->pair_blocks != 1 && t->pair_blocks != 2 && t->pair_blocks != 4)
     return fail(h, IDPD_ERR_INVALID_ARG, "pair_blocks must be 1, 2 or 4 (0: 1)");
+  if (t->density_lanes != 0 && t->density_lanes != 8 && t->density_lanes != 16 &&
+      t->density_lanes != 32)
+    return fail(h, IDPD_ERR_INVALID_ARG, "density_lanes must be 8, 16 or 32 (0: 32)");
   if (!(t->skin >= 0.0f && t->skin < 1.0f))
     return fail(h, IDPD_ERR_INVALID_ARG, "skin must be in [0, 1)");
   for (int r = 0; r < h->R; r++)
@@ -1574,7 +1577,10 @@ int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
   cudaSetDevice(h->device);
   const bool changed = t->reach != h->tune.reach || t->skin != h->tune.skin;
   const int lanes = t->pair_lanes ? t->pair_lanes : 16, fblk = t->pair_blocks ? t->pair_blocks : 1;
-  if (lanes != h->tune.lanes || fblk != h->tune.fblk) invalidate_graph(h);
+  const int dlanes = t->density_lanes ? t->density_lanes : 32;
+  if (lanes != h->tune.lanes || fblk != h->tune.fblk || dlanes != h->tune.dlanes)
+    invalidate_graph(h);
+  h->tune.dlanes = dlanes;
   h->tune.lanes = lanes;
   h->tune.fblk = fblk;
   h->tune.reach = t->reach;
@@ -1595,6 +1601,7 @@ int idpd_get_tuning(const idpd_handle* h, idpd_tuning* t) {
   t->skin = h->tune.skin;
   t->pair_lanes = h->tune.lanes;
   t->pair_blocks = h->tune.fblk;
+  t->density_lanes = h->tune.dlanes;
   return IDPD_OK;
 }
 
@@ -1749,7 +1756,7 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   if (verlet) launch_verlet_build(d, h->nblk, h->tune.reach, h->st);
   CK(cudaEventRecord(ev[4], h->st));
   h->pairs_valid = true;
-  launch_density(d, h->nblk, mode, h->tune.reach, verlet, false, h->cap, h->st);
+  launch_density(d, h->nblk, mode, h->tune.reach, verlet, false, h->cap, h->st, h->tune.dlanes);
   CK(cudaEventRecord(ev[5], h->st));
   launch_force(d, h->nblk, mode, false, verlet, h->tune, form_mask(h), h->cap, h->st);
   CK(cudaEventRecord(ev[6], h->st));

@@ -256,21 +256,6 @@ __device__ __forceinline__ void eval_pair(const DevState& d, const RepDev* R, co
   if (OTHER) add_to_other<PRESS>(d, t, g);
 }
 
-// Sorts the 32 keys of a warp ascending (bitonic network over the lanes).
-__device__ __forceinline__ uint32_t warp_sort_asc(uint32_t key, int lane) {
-#pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const uint32_t other = __shfl_xor_sync(0xffffffffu, key, j);
-      const bool up = (lane & k) == 0 || k == 32;
-      const bool low = (lane & j) == 0;
-      key = (low == up) ? min(key, other) : max(key, other);
-    }
-  }
-  return key;
-}
-
 // The total of parts c over the LP lanes of group g (lanes LP g .. LP g + LP - 1).
 template <int LP>
 __device__ __forceinline__ long long group_total(const PartSums& P, int c, int g) {

@@ -264,6 +264,133 @@ __global__ void __launch_bounds__(kRowBlock, (MODE != kDensSweep && (REACH == 2 
   }
 }
 
+// Pass 1 over the kept lists with LP lanes per particle (LP 8 or 16; 32 is
+// k_density_f32's kDensKept form): for systems whose kept lists are short
+// (a liquid at density 6 keeps ~20 owned candidates per particle), one warp
+// per particle leaves most lanes idle and repeats the per-particle work (its
+// row, the totals of its weights, its counts) for every particle. The warp
+// sorts its 32 rows by kept-list length (as pass 2 does) and takes them
+// 32 / LP at a time. Per candidate it does what k_density_f32 does over a
+// kept list, and the pass-2 list comes out in the same order, so every LP
+// gives the same densities and lists bit for bit. Rows whose kept list
+// overflowed are left to kDensKeptOver.
+template <int REACH, bool MARKS, int LP>
+__global__ void __launch_bounds__(kRowBlock, 8) k_density_kept_lp(DevState d) {
+  constexpr int G = 32 / LP;  // particles per warp at a time
+  const int r = d.blk_rep[blockIdx.x];
+  const RepDev* R = d.reps + r;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int h = lane / LP, sl = lane % LP;
+  const int s0 = d.blk_row[blockIdx.x] + 32 * wid;
+  const int s_end = min(s0 + 32, R->row_off + R->n);
+  if (s0 >= s_end) return;
+  const bool warren = R->form == IDPD_FORM_WARREN_K;
+  const float cutd2 = R->wrd * R->wrd;  // density cutoff^2 (1 unless Warren)
+  const double cutd2d = (double)R->wrd * (double)R->wrd;
+  const float inv_rd = R->winv_rd, wnorm = R->wnorm, pre = R->dens_prescale;
+  const float csx = R->cs_f[0], csy = R->cs_f[1], csz = R->cs_f[2];
+  const bool prec = MARKS && R->prec_on;
+  const uint32_t gmask = (LP == 32 ? 0xffffffffu : ((1u << LP) - 1u)) << (LP * h);
+  const uint32_t group_lt = ((1u << lane) - 1u) & gmask;
+  // the chunk's rows sorted by kept-list length (rows past the end and
+  // overflowed lists count 0): key = length << 5 | row - s0
+  uint32_t key;
+  {
+    const int sk = s0 + lane;
+    const uint32_t c = sk < s_end ? (uint32_t)d.vn[sk] : 0u;
+    key = ((c != kNbrFallback ? c : 0u) << 5) | (uint32_t)lane;
+    key = warp_sort_asc(key, lane);
+  }
+  for (int i2 = 0; i2 < 32; i2 += G) {
+    const int s2 = s0 + (int)(__shfl_sync(0xffffffffu, key, i2 + h) & 31u);
+    const uint32_t nv0 = s2 < s_end ? (uint32_t)d.vn[s2] : kNbrFallback;
+    const bool act = nv0 != kNbrFallback;
+    if (!__any_sync(0xffffffffu, act)) continue;
+    const int s = s2 < s_end ? s2 : s0;
+    const int nv = act ? (int)nv0 : 0;
+    int nmax = nv;  // rounds of the warp: the longest list of its groups
+#pragma unroll
+    for (int o = LP; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+    const float4 pi = d.posf[s];
+    const uint32_t si = d.perm[s], pri = fbits(pi.w);
+    int nl = 0;  // owned pairs within the cutoff
+    bool hit = false;
+    uint32_t q0 = 0, q1 = 0, q2 = 0;
+    const uint32_t* vl = d.vl + (size_t)s * kVerletCap;
+    uint32_t* out = d.nbl + (size_t)s * kNbrCap;
+    uint32_t e_next = sl < nv ? vl[sl] : 0u;  // one round ahead
+    for (int k0 = 0; k0 < nmax; k0 += LP) {
+      const int k = k0 + sl;
+      const bool valid = k < nv;
+      const uint32_t e = e_next;
+      if (k + LP < nv) e_next = vl[k + LP];
+      int t, dx, dy, dz;
+      read_entry(e, t, dx, dy, dz);
+      if (!valid) t = s;
+      const float4 pj = __ldg(d.posf + t);
+      const float ex = (pi.x - (float)dx * csx) - pj.x;
+      const float ey = (pi.y - (float)dy * csy) - pj.y;
+      const float ez = (pi.z - (float)dz * csz) - pj.z;
+      const float dr2 = ex * ex + ey * ey + ez * ez;
+      bool in1 = valid && dr2 < 1.0f;
+      bool ind = in1 && dr2 < cutd2 && dr2 >= 1.0e-10f;
+      const bool near1 = valid && fabsf(dr2 - 1.0f) <= kGuard;
+      const bool near2 = valid && ((warren && fabsf(dr2 - cutd2) <= kGuard) || dr2 < 1.0e-10f);
+      // rare: the FP64 decisions of the reference near the cutoffs and at
+      // coincident positions
+      if (__any_sync(0xffffffffu, near1 || near2)) {
+        if (near1 || near2) {
+          const double e2 = exact_dr2(d, R, si, d.perm[t]);
+          if (near1) in1 = e2 < 1.0;
+          ind = in1 && (near2 ? (e2 < cutd2d && e2 != 0.0) : (dr2 < cutd2 && dr2 >= 1.0e-10f));
+        }
+      }
+      const uint32_t prj = fbits(pj.w);
+      if (ind) {
+        const uint32_t w = dens_weight(dr2, warren, inv_rd, wnorm, pre);
+        add_weight(q0, q1, q2, prj, w);
+        atomicAdd(d.dsum + 4 * (size_t)t + (pri & 3u), (unsigned long long)w);
+      }
+      if (MARKS && prec && in1) {
+        hit |= pri == R->prec_from && prj == R->prec_near;
+        if (prj == R->prec_from && pri == R->prec_near) d.phit[t] = 1;
+      }
+      const uint32_t mask = __ballot_sync(0xffffffffu, in1);
+      if (in1) {
+        const int pos = nl + __popc(mask & group_lt);
+        if (pos < kNbrCap) out[pos] = e;
+      }
+      nl += __popc(mask & gmask);
+    }
+    // the totals of each group's lanes: a kept list holds at most kVerletCap
+    // (512) candidates, each weight is below 2^23, so a total is below 2^32
+    uint32_t a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      const uint32_t t0 = __reduce_add_sync(0xffffffffu, h == g ? q0 : 0u);
+      const uint32_t t1 = __reduce_add_sync(0xffffffffu, h == g ? q1 : 0u);
+      const uint32_t t2 = __reduce_add_sync(0xffffffffu, h == g ? q2 : 0u);
+      if (h == g) {
+        a0 = t0;
+        a1 = t1;
+        a2 = t2;
+      }
+    }
+    if (MARKS) hit = (__ballot_sync(0xffffffffu, hit) & gmask) != 0u;
+    if (sl == 0 && act) {
+      unsigned long long* q = d.dsum + 4 * (size_t)s;
+      if (a0) atomicAdd(q, (unsigned long long)a0);
+      if (a1) atomicAdd(q + 1, (unsigned long long)a1);
+      if (a2) atomicAdd(q + 2, (unsigned long long)a2);
+      d.nbn[s] = nl <= kNbrCap ? (uint16_t)nl : (uint16_t)kNbrFallback;
+      d.npair[s] = 2u * (uint32_t)nl;  // ordered pairs: each owned pair counts twice
+      if (MARKS && hit) d.phit[s] = 1;
+    }
+    __syncwarp();
+  }
+}
+static_assert((long long)kVerletCap * (1ll << 23) <= (1ll << 32), "32-bit totals of pass 1");
+
 // The FP32 densities of pass 1 from its fixed-point sums (and the fixed-point
 // densities of the fine-grained API); the sums are zeroed for the next pass.
 __global__ void __launch_bounds__(kRowBlock) k_dens_finalize(DevState d) {
@@ -508,10 +635,15 @@ __global__ void __launch_bounds__(kRowBlock) k_density_f64(DevState d) {
 }
 
 template <int REACH, bool MARKS>
-void launch_density_reach(const DevState& d, int nblk, bool verlet, cudaStream_t st) {
+void launch_density_reach(const DevState& d, int nblk, bool verlet, int lanes, cudaStream_t st) {
   constexpr size_t sm = dens_sweep_smem_bytes();
   if (verlet) {
-    k_density_f32<REACH, kDensKept, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
+    if (lanes == 8)
+      k_density_kept_lp<REACH, MARKS, 8><<<nblk, kRowBlock, 0, st>>>(d);
+    else if (lanes == 16)
+      k_density_kept_lp<REACH, MARKS, 16><<<nblk, kRowBlock, 0, st>>>(d);
+    else
+      k_density_f32<REACH, kDensKept, MARKS><<<nblk, kRowBlock, 0, st>>>(d);
     k_density_f32<REACH, kDensKeptOver, MARKS><<<nblk, kRowBlock, sm, st>>>(d);
   } else {
     k_density_f32<REACH, kDensSweep, MARKS><<<nblk, kRowBlock, sm, st>>>(d);
@@ -519,11 +651,12 @@ void launch_density_reach(const DevState& d, int nblk, bool verlet, cudaStream_t
 }
 
 template <bool MARKS>
-void launch_density_f32(const DevState& d, int nblk, int reach, bool verlet, cudaStream_t st) {
+void launch_density_f32(const DevState& d, int nblk, int reach, bool verlet, int lanes,
+                        cudaStream_t st) {
   if (reach == 2)
-    launch_density_reach<2, MARKS>(d, nblk, verlet, st);
+    launch_density_reach<2, MARKS>(d, nblk, verlet, lanes, st);
   else
-    launch_density_reach<1, MARKS>(d, nblk, verlet, st);
+    launch_density_reach<1, MARKS>(d, nblk, verlet, lanes, st);
 }
 
 // The reference's pair expression in FP64 (nbdf_calculator.hpp:84-132): the
@@ -909,7 +1042,7 @@ void launch_force_fp64(const DevState& d, int nblk, int mode, bool with_press, b
 }
 
 void launch_density(const DevState& d, int nblk, int mode, int reach, bool verlet, bool marks,
-                    size_t rows, cudaStream_t st) {
+                    size_t rows, cudaStream_t st, int lanes) {
   if (nblk == 0) return;
   if (mode == kPairsF64) {
     k_density_f64<<<nblk, kRowBlock, 0, st>>>(d);
@@ -925,9 +1058,9 @@ void launch_density(const DevState& d, int nblk, int mode, int reach, bool verle
   }
   if (marks) {
     cudaMemsetAsync(d.phit, 0, rows, st);
-    launch_density_f32<true>(d, nblk, reach, verlet, st);
+    launch_density_f32<true>(d, nblk, reach, verlet, lanes, st);
   } else {
-    launch_density_f32<false>(d, nblk, reach, verlet, st);
+    launch_density_f32<false>(d, nblk, reach, verlet, lanes, st);
   }
   k_dens_finalize<<<nblk, kRowBlock, 0, st>>>(d);
 }

@@ -15,6 +15,21 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
   return v;
 }
 
+// Sorts the 32 keys of a warp ascending (bitonic network over the lanes).
+__device__ __forceinline__ uint32_t warp_sort_asc(uint32_t key, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t other = __shfl_xor_sync(0xffffffffu, key, j);
+      const bool up = (lane & k) == 0 || k == 32;
+      const bool low = (lane & j) == 0;
+      key = (low == up) ? min(key, other) : max(key, other);
+    }
+  }
+  return key;
+}
+
 // FP64 squared distance of rows i and j in the reference's operation order
 // (nbdf_calculator.hpp:27-29, 86-87), j shifted to its image nearest to i.
 // The image follows from the positions themselves, so it stays right while

@@ -174,11 +174,13 @@ struct PairTuning {
   float skin;      // > 0: lists of pairs within 1 + skin kept until a rebuild (reach 1)
   int lanes;       // pass 2: lanes per particle (8, 16 or 32)
   int fblk;        // pass 2: 128-row blocks per CTA (1, 2 or 4)
+  int dlanes;      // pass 1 over kept lists: lanes per particle (8, 16 or 32)
 };
 // Pass 1 and its densities (verlet: over the kept lists; marks: also the
 // precursor marks, zeroed first over rows, the buffer's capacity).
+// (lanes: lanes per particle of the kept-list pass, 8, 16 or 32)
 void launch_density(const DevState& d, int nblk, int mode, int reach, bool verlet, bool marks,
-                    size_t rows, cudaStream_t st);
+                    size_t rows, cudaStream_t st, int lanes = 32);
 // Precursor conversion after the force pass (marks: the FP32 pass 1 left its
 // marks; else the cells are swept).
 void launch_precursor(const DevState& d, int nblk, bool marks, cudaStream_t st);

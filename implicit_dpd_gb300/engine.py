@@ -334,15 +334,17 @@ class Engine:
                                             C.cast(ptrs, C.c_void_p)), "retrieve_walks")
         return out
 
-    def set_tuning(self, reach, skin=None, lanes=None, blocks=None):
+    def set_tuning(self, reach, skin=None, lanes=None, blocks=None, dens_lanes=None):
         """reach 1 or 2; skin > 0 keeps the neighbour lists between rebuilds;
-        lanes (8, 16, 32) and blocks (1, 2, 4) shape the force pass (None:
-        keep the current value)."""
+        lanes (8, 16, 32) and blocks (1, 2, 4) shape the force pass, dens_lanes
+        (8, 16, 32) the density pass over kept lists (None: keep the current
+        value)."""
         cur = IdpdTuning()
         self._ck(self.L.idpd_get_tuning(self.h, C.byref(cur)), "get_tuning")
         t = IdpdTuning(reach=reach, skin=cur.skin if skin is None else skin,
                        pair_lanes=cur.pair_lanes if lanes is None else lanes,
-                       pair_blocks=cur.pair_blocks if blocks is None else blocks)
+                       pair_blocks=cur.pair_blocks if blocks is None else blocks,
+                       density_lanes=cur.density_lanes if dens_lanes is None else dens_lanes)
         self._ck(self.L.idpd_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def tuning(self):
@@ -350,7 +352,7 @@ class Engine:
         t = IdpdTuning()
         self._ck(self.L.idpd_get_tuning(self.h, C.byref(t)), "get_tuning")
         return {"reach": t.reach, "skin": round(float(t.skin), 6), "lanes": t.pair_lanes,
-                "blocks": t.pair_blocks}
+                "blocks": t.pair_blocks, "dens_lanes": t.density_lanes}
 
     def set_precursor(self, prop_from, prop_near, prop_to, threshold, seed, replica=0,
                       enabled=True):

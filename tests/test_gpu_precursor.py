@@ -18,13 +18,13 @@ pytestmark = pytest.mark.gpu
 SEED = 4242
 
 
-def _engine(p, st, n_amp, flags=0, skin=0.0):
+def _engine(p, st, n_amp, flags=0, skin=0.0, dens_lanes=32):
     e = Engine(flags=flags)
     e.set_params(p)
     e.upload(st)
     e.build_topology(n_amp, [0, 3])
     if skin:
-        e.set_tuning(1, skin)
+        e.set_tuning(1, skin, dens_lanes=dens_lanes)
     return e
 
 
@@ -45,12 +45,13 @@ def _check_steps(e, p, steps, thr):
     return total
 
 
-@pytest.mark.parametrize("flags,skin", [(0, 0.0), (0, 0.2), (CFG_FP64_PAIRS, 0.0)])
-def test_precursor_decisions_match_oracle(flags, skin):
+@pytest.mark.parametrize("flags,skin,dens_lanes", [(0, 0.0, 32), (0, 0.2, 32), (0, 0.2, 16),
+                                                   (0, 0.2, 8), (CFG_FP64_PAIRS, 0.0, 32)])
+def test_precursor_decisions_match_oracle(flags, skin, dens_lanes):
     box, st, n_amp = mixed_system(seed=12)
     p = mdpd_params(box, time=300)
     thr = precursor_threshold(0.05)
-    e = _engine(p, st, n_amp, flags, skin)
+    e = _engine(p, st, n_amp, flags, skin, dens_lanes)
     e.set_precursor(SOLVENT, HYPHOB, HYPHIL, thr, SEED)
     total = _check_steps(e, p, 6, thr)
     assert total > 20

@@ -14,6 +14,41 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(16, 1), (8, 1), (32, 1), (16, 2), (16, 4), (8, 4), (32, 2)]
 
 
+def test_density_lanes_give_the_same_trajectory():
+    # the density pass over kept lists with 32, 16 or 8 lanes per particle:
+    # the same densities, pass-2 lists and hence trajectories bit for bit
+    box, st, n_amp = mixed_system(seed=23)
+    p = mdpd_params(box, time=13)
+    out = []
+    for dl in (32, 16, 8):
+        e = Engine(sort_period=9)
+        e.set_params(p)
+        e.upload(st)
+        e.build_topology(n_amp)
+        e.set_tuning(1, 0.2, dens_lanes=dl)
+        assert e.tuning()["dens_lanes"] == dl
+        e.step(30)
+        out.append((e.download(), e.list_rebuilds(), e.pair_count()))
+        e.close()
+    for (s, rb, pc), dl in zip(out[1:], (16, 8)):
+        for k in ("pos", "vel", "acc"):
+            assert np.array_equal(s[k], out[0][0][k]), (dl, k)
+        assert rb == out[0][1] and pc == out[0][2], dl
+    # Warren liquids in a batched handle
+    reps = [configs.liquid(np.array([7.0, 7.5, 8.0]), 5.0, seed=s) for s in (1, 2)]
+    res = []
+    for dl in (32, 8):
+        e = Engine(n_replicas=2)
+        for r, rs in enumerate(reps):
+            e.set_params(warren_params(np.array([7.0, 7.5, 8.0]), seed=5 + r), replica=r)
+            e.upload(rs, replica=r)
+        e.set_tuning(1, 0.25, dens_lanes=dl)
+        e.step(20)
+        res.append([e.download(replica=r)["pos"] for r in range(2)])
+        e.close()
+    assert all(np.array_equal(a, b) for a, b in zip(res[0], res[1]))
+
+
 def test_every_shape_gives_the_same_forces_and_trajectory():
     box, st, n_amp = mixed_system(seed=21)
     p = mdpd_params(box, time=11)
