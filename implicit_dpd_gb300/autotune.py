@@ -16,9 +16,9 @@ import os
 DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
                    (2, 0.3))
 # (lanes per particle, row blocks per CTA) of the force pass; the first is the default
-SHAPES = ((16, 1), (8, 1), (32, 1), (8, 2), (16, 2))
+SHAPES = ((16, 1), (8, 1), (32, 1), (8, 2), (16, 2), (4, 1), (4, 2))
 # lanes per particle of the density pass over kept lists; the first is the default
-DENS_LANES = (32, 16, 8)
+DENS_LANES = (32, 16, 8, 4)
 
 
 def default_cache_path():
@@ -56,7 +56,7 @@ def _store(path, table):
 
 
 def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, refresh=False,
-         shapes=SHAPES, dens_lanes=DENS_LANES):
+         shapes=SHAPES, dens_lanes=DENS_LANES, rounds=2):
     """Applies the fastest (reach, skin), then the fastest force-pass shape
     (lanes, blocks) at that (reach, skin), then the fastest density-pass lanes
     (with kept lists), to `engine` and returns (choice, times): choice =
@@ -65,7 +65,8 @@ def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, r
     step (empty when the choice came from the cache). With a key and a cache
     path, a cached choice is applied without timing unless refresh is set,
     and a new choice is written back. Choices whose skin the box does not
-    allow are skipped."""
+    allow are skipped; the launch shapes and the density lanes are timed
+    `rounds` times each, in rounds over the candidates, keeping the fastest."""
     table = _load(cache_path) if (cache_path and key) else {}
     if key and not refresh and key in table:
         c = table[key]
@@ -93,16 +94,23 @@ def tune(engine, choices=DEFAULT_CHOICES, steps=40, key=None, cache_path=None, r
     if not times:
         raise ValueError("no tuning choice fits this system")
     reach, skin = min(times, key=times.get)
-    shape_times = {shapes[0]: times[(reach, skin)]}
-    for lanes, blocks in shapes[1:]:
-        engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl0)
-        shape_times[(lanes, blocks)] = timed()
+    # the launch shapes differ by a few per cent, about the spread of one
+    # timing (the list rebuilds it catches): each is timed twice, in two
+    # rounds over the candidates, and keeps its faster time
+    shape_times = {}
+    for _ in range(rounds):
+        for lanes, blocks in shapes:
+            engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl0)
+            t = timed()
+            shape_times[(lanes, blocks)] = min(t, shape_times.get((lanes, blocks), t))
     lanes, blocks = min(shape_times, key=shape_times.get)
     dens_times = {dl0: shape_times[(lanes, blocks)]}
     if skin > 0:  # the density pass's lanes act on the kept lists only
-        for dl in dens_lanes[1:]:
-            engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
-            dens_times[dl] = timed()
+        for _ in range(rounds):
+            for dl in dens_lanes:
+                engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
+                t = timed()
+                dens_times[dl] = min(t, dens_times.get(dl, t))
     dl = min(dens_times, key=dens_times.get)
     engine.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
     choice = {"reach": reach, "skin": skin, "lanes": lanes, "blocks": blocks, "dens_lanes": dl}

@@ -1559,13 +1559,14 @@ int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t) {
   if (t->reach < 1 || t->reach > 2) return fail(h, IDPD_ERR_INVALID_ARG, "reach must be 1 or 2");
   if (t->reach != 1 && (h->flags & IDPD_CFG_FP64_KEPT))
     return fail(h, IDPD_ERR_INVALID_ARG, "the FP64 engine-algorithm arm runs at reach 1");
-  if (t->pair_lanes != 0 && t->pair_lanes != 8 && t->pair_lanes != 16 && t->pair_lanes != 32)
-    return fail(h, IDPD_ERR_INVALID_ARG, "pair_lanes must be 8, 16 or 32 (0: 16)");
+  if (t->pair_lanes != 0 && t->pair_lanes != 4 && t->pair_lanes != 8 && t->pair_lanes != 16 &&
+      t->pair_lanes != 32)
+    return fail(h, IDPD_ERR_INVALID_ARG, "pair_lanes must be 4, 8, 16 or 32 (0: 16)");
   if (t->pair_blocks != 0 && t->pair_blocks != 1 && t->pair_blocks != 2 && t->pair_blocks != 4)
     return fail(h, IDPD_ERR_INVALID_ARG, "pair_blocks must be 1, 2 or 4 (0: 1)");
-  if (t->density_lanes != 0 && t->density_lanes != 8 && t->density_lanes != 16 &&
-      t->density_lanes != 32)
-    return fail(h, IDPD_ERR_INVALID_ARG, "density_lanes must be 8, 16 or 32 (0: 32)");
+  if (t->density_lanes != 0 && t->density_lanes != 4 && t->density_lanes != 8 &&
+      t->density_lanes != 16 && t->density_lanes != 32)
+    return fail(h, IDPD_ERR_INVALID_ARG, "density_lanes must be 4, 8, 16 or 32 (0: 32)");
   if (!(t->skin >= 0.0f && t->skin < 1.0f))
     return fail(h, IDPD_ERR_INVALID_ARG, "skin must be in [0, 1)");
   for (int r = 0; r < h->R; r++)

@@ -592,7 +592,9 @@ void launch_force_form(const DevState& d, int nblk, bool with_press, const PairT
     return;
   }
   const int fb = tu.fblk == 2 || tu.fblk == 4 ? tu.fblk : 1;
-  if (tu.lanes == 8)
+  if (tu.lanes == 4)
+    launch_force_shape<FORM, false, 4>(d, nblk, tu.reach, kept, fb, st);
+  else if (tu.lanes == 8)
     launch_force_shape<FORM, false, 8>(d, nblk, tu.reach, kept, fb, st);
   else if (tu.lanes == 32)
     launch_force_shape<FORM, false, 32>(d, nblk, tu.reach, kept, fb, st);

@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kRowBlock, (MODE != kDensSweep && (REACH == 2 
   }
 }
 
-// Pass 1 over the kept lists with LP lanes per particle (LP 8 or 16; 32 is
+// Pass 1 over the kept lists with LP lanes per particle (LP 4, 8 or 16; 32 is
 // k_density_f32's kDensKept form): for systems whose kept lists are short
 // (a liquid at density 6 keeps ~20 owned candidates per particle), one warp
 // per particle leaves most lanes idle and repeats the per-particle work (its
@@ -638,7 +638,9 @@ template <int REACH, bool MARKS>
 void launch_density_reach(const DevState& d, int nblk, bool verlet, int lanes, cudaStream_t st) {
   constexpr size_t sm = dens_sweep_smem_bytes();
   if (verlet) {
-    if (lanes == 8)
+    if (lanes == 4)
+      k_density_kept_lp<REACH, MARKS, 4><<<nblk, kRowBlock, 0, st>>>(d);
+    else if (lanes == 8)
       k_density_kept_lp<REACH, MARKS, 8><<<nblk, kRowBlock, 0, st>>>(d);
     else if (lanes == 16)
       k_density_kept_lp<REACH, MARKS, 16><<<nblk, kRowBlock, 0, st>>>(d);

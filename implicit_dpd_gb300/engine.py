@@ -336,8 +336,8 @@ class Engine:
 
     def set_tuning(self, reach, skin=None, lanes=None, blocks=None, dens_lanes=None):
         """reach 1 or 2; skin > 0 keeps the neighbour lists between rebuilds;
-        lanes (8, 16, 32) and blocks (1, 2, 4) shape the force pass, dens_lanes
-        (8, 16, 32) the density pass over kept lists (None: keep the current
+        lanes (4, 8, 16, 32) and blocks (1, 2, 4) shape the force pass,
+        dens_lanes (4, 8, 16, 32) the density pass over kept lists (None: keep the current
         value)."""
         cur = IdpdTuning()
         self._ck(self.L.idpd_get_tuning(self.h, C.byref(cur)), "get_tuning")

@@ -422,10 +422,10 @@ typedef struct idpd_tuning {
                            side >= 3 (rc + skin)). Pair sets stay exact; sums differ
                            from skin 0 only by FP32 rounding of the cell-local
                            coordinates. 0: cells and lists every step. */
-  int32_t pair_lanes;   /* pass 2: lanes per particle, 8, 16 or 32 (0: 16)        */
+  int32_t pair_lanes;   /* pass 2: lanes per particle, 4, 8, 16 or 32 (0: 16)     */
   int32_t pair_blocks;  /* pass 2: 128-row blocks per CTA, 1, 2 or 4 (0: 1)        */
-  int32_t density_lanes; /* pass 1 over kept lists: lanes per particle, 8, 16 or 32
-                            (0: 32); fewer suit short lists (liquids)             */
+  int32_t density_lanes; /* pass 1 over kept lists: lanes per particle, 4, 8, 16 or
+                            32 (0: 32); fewer suit short lists (liquids)          */
   int32_t reserved[3];
 } idpd_tuning;
 int idpd_set_tuning(idpd_handle* h, const idpd_tuning* t);

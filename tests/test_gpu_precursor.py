@@ -46,7 +46,8 @@ def _check_steps(e, p, steps, thr):
 
 
 @pytest.mark.parametrize("flags,skin,dens_lanes", [(0, 0.0, 32), (0, 0.2, 32), (0, 0.2, 16),
-                                                   (0, 0.2, 8), (CFG_FP64_PAIRS, 0.0, 32)])
+                                                   (0, 0.2, 8), (0, 0.2, 4),
+                                                   (CFG_FP64_PAIRS, 0.0, 32)])
 def test_precursor_decisions_match_oracle(flags, skin, dens_lanes):
     box, st, n_amp = mixed_system(seed=12)
     p = mdpd_params(box, time=300)

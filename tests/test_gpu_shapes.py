@@ -1,5 +1,6 @@
 """Launch shapes of the force pass (idpd_tuning.pair_lanes, pair_blocks):
-lanes per particle 8, 16 or 32 and 1, 2 or 4 row blocks per CTA. Every
+lanes per particle 4, 8, 16 or 32 and 1, 2 or 4 row blocks per CTA, and the
+density pass's lanes per particle over kept lists (density_lanes). Every
 shape evaluates the same pairs into the same fixed-point sums, so forces and
 trajectories must be equal bit for bit; a CTA whose row blocks belong to
 different replicas (and pair forms) must keep each block's tables."""
@@ -11,7 +12,7 @@ from implicit_dpd_gb300 import configs
 from implicit_dpd_gb300.engine import Engine, EngineError
 
 pytestmark = pytest.mark.gpu
-SHAPES = [(16, 1), (8, 1), (32, 1), (16, 2), (16, 4), (8, 4), (32, 2)]
+SHAPES = [(16, 1), (8, 1), (32, 1), (16, 2), (16, 4), (8, 4), (32, 2), (4, 1), (4, 2)]
 
 
 def test_density_lanes_give_the_same_trajectory():
@@ -20,7 +21,7 @@ def test_density_lanes_give_the_same_trajectory():
     box, st, n_amp = mixed_system(seed=23)
     p = mdpd_params(box, time=13)
     out = []
-    for dl in (32, 16, 8):
+    for dl in (32, 16, 8, 4):
         e = Engine(sort_period=9)
         e.set_params(p)
         e.upload(st)
@@ -30,14 +31,14 @@ def test_density_lanes_give_the_same_trajectory():
         e.step(30)
         out.append((e.download(), e.list_rebuilds(), e.pair_count()))
         e.close()
-    for (s, rb, pc), dl in zip(out[1:], (16, 8)):
+    for (s, rb, pc), dl in zip(out[1:], (16, 8, 4)):
         for k in ("pos", "vel", "acc"):
             assert np.array_equal(s[k], out[0][0][k]), (dl, k)
         assert rb == out[0][1] and pc == out[0][2], dl
     # Warren liquids in a batched handle
     reps = [configs.liquid(np.array([7.0, 7.5, 8.0]), 5.0, seed=s) for s in (1, 2)]
     res = []
-    for dl in (32, 8):
+    for dl in (32, 4):
         e = Engine(n_replicas=2)
         for r, rs in enumerate(reps):
             e.set_params(warren_params(np.array([7.0, 7.5, 8.0]), seed=5 + r), replica=r)
