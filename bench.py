@@ -551,7 +551,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     several ranks the replicas are dealt out by LPT on their particle counts
     (no exchange while stepping); the job's rate is all particles x steps
     over the slowest rank's time. Returns particle-steps/s of both forms."""
-    from implicit_dpd_gb300.abi import CFG_STEP_PER_LAUNCH
+    from implicit_dpd_gb300.abi import CFG_PLAIN_GRAPHS
     from implicit_dpd_gb300.engine import Engine
     from implicit_dpd_gb300.partition import imbalance, lpt_partition
 
@@ -591,7 +591,7 @@ def replicas_bench(steps=50, n_rep=256, device=0, rank=0, world=1, dist=None):
     eb.step(steps)  # the steps in one graph launch (the step in a WHILE node)
     batched = n_tot * steps / (dist.max(eb.last_step_ms()) * 1e-3)
     # the same batch with one graph launch per step
-    ep = Engine(n_replicas=len(mine), device=device, flags=CFG_STEP_PER_LAUNCH)
+    ep = Engine(n_replicas=len(mine), device=device, flags=CFG_PLAIN_GRAPHS)
     for k in range(len(mine)):
         upload(ep, k, k)
     ep.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dlanes)
@@ -673,12 +673,17 @@ def run_kernel_case(path, device=0, reach=0, skin=None):
     e.close()
 
 
+# IDPD_CFG_PLAIN_GRAPHS with --plain-graphs: one graph launch per step and no
+# conditional nodes, the form whose kernels ncu can trace (the same results)
+GRAPH_FLAGS = 0
+
+
 def make_engine(st, n_amp, rp, flags=0, device=0):
     from implicit_dpd_gb300.engine import Engine, derive_params
 
     p = derive_params(rp)
     p.seed, p.time = 12345, 1
-    e = Engine(flags=flags, sort_period=100, device=device)
+    e = Engine(flags=flags | GRAPH_FLAGS, sort_period=100, device=device)
     e.set_params(p)
     e.upload(st)
     e.build_topology(n_amp)
@@ -955,6 +960,8 @@ def main():
     ap.add_argument("--layers", type=int, default=N_LAYERS, help="bilayers stacked along z")
     ap.add_argument("--save-state", default=None,
                     help="write the equilibrated state (npz) for --kernel-case")
+    ap.add_argument("--plain-graphs", action="store_true",
+                    help="one graph launch per step and no conditional nodes (for ncu)")
     ap.add_argument("--kernel-case", default=None,
                     help="load a saved state and run three graph steps (profiling case)")
     ap.add_argument("--reach", type=int, default=0,
@@ -966,6 +973,11 @@ def main():
     ap.add_argument("--blocks", type=int, default=1,
                     help="force pass: 128-row blocks per CTA with --reach (1, 2 or 4)")
     args = ap.parse_args()
+    if args.plain_graphs:
+        from implicit_dpd_gb300.abi import CFG_PLAIN_GRAPHS
+
+        global GRAPH_FLAGS
+        GRAPH_FLAGS = CFG_PLAIN_GRAPHS
     rank, world, local_rank = dist_env()
     if args.kernel_case:
         run_kernel_case(args.kernel_case, local_rank, args.reach,

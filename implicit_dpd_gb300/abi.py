@@ -23,7 +23,7 @@ STATUS_NAMES = {
 CFG_FP64_PAIRS = 0x1
 CFG_FP64_KEPT = 0x4
 CFG_TIMING = 0x2
-CFG_STEP_PER_LAUNCH = 0x8  # one graph launch per step (default: K steps in one launch)
+CFG_PLAIN_GRAPHS = 0x8  # one graph launch per step, no conditional nodes (same results)
 
 NONE32 = 0xFFFFFFFF  # amp_id / unit of solvent beads (parameter.hpp:450-451)
 

@@ -715,7 +715,8 @@ IfScope begin_if(idpd_handle* h, Cond&& cond) {
   const cudaGraphNode_t* deps = nullptr;
   const cudaGraphEdgeData* edges = nullptr;
   size_t nd = 0;
-  if (cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd) != cudaSuccess ||
+  if ((h->flags & IDPD_CFG_PLAIN_GRAPHS) ||
+      cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, &edges, &nd) != cudaSuccess ||
       cs != cudaStreamCaptureStatusActive)
     return {h->st, false};
   cudaGraphConditionalHandle ch;
@@ -1427,7 +1428,7 @@ int idpd_step(idpd_handle* h, int32_t nsteps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, IDPD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
-  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_STEP_PER_LAUNCH) && !h->loop_failed;
+  const bool loop = nsteps > 1 && !(h->flags & IDPD_CFG_PLAIN_GRAPHS) && !h->loop_failed;
   if (loop && !h->graph_loop && !build_loop_graph(h)) h->loop_failed = true;
   const bool use_loop = loop && h->graph_loop;
   // whether the step `ahead` steps from now observes: some replica's step

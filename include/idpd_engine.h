@@ -111,11 +111,15 @@ typedef struct idpd_config {
  * sums) with FP64 pair arithmetic: the FP32 engine's denominator with the
  * algorithm held fixed. Cell reach 1 only; excludes IDPD_CFG_FP64_PAIRS. */
 #define IDPD_CFG_FP64_KEPT 0x4
-/* idpd_step(h, K) launches one graph per step. By default the K steps go to
- * the device in one launch: a graph whose conditional WHILE node repeats the
- * captured step K times (between storage reorders and observing steps).
- * Results are the same either way. */
-#define IDPD_CFG_STEP_PER_LAUNCH 0x8
+/* Plain graphs: idpd_step(h, K) launches one graph per step, and the step's
+ * graph holds no conditional nodes (every gated kernel is launched and skips
+ * itself). By default the K steps go to the device in one launch, a graph
+ * whose conditional WHILE node repeats the captured step K times (between
+ * storage reorders and observing steps), and the step's rarely needed work
+ * (the cell and list rebuild, the drift removal) sits in conditional IF
+ * nodes. Results are the same either way; profilers that cannot trace the
+ * kernels of graphs with conditional nodes need the plain form. */
+#define IDPD_CFG_PLAIN_GRAPHS 0x8
 
 int idpd_create(const idpd_config* cfg, idpd_handle** out);
 int idpd_destroy(idpd_handle* h);
@@ -195,7 +199,7 @@ int idpd_remove_cmdrift(idpd_handle* h);
  * to the next storage reorder or observing step go to the device in one
  * launch (the graph's conditional WHILE node repeats the step, and ends the
  * loop after a step whose reaction event stopped the run); an observing step
- * is one launch, and with IDPD_CFG_STEP_PER_LAUNCH every step is.
+ * is one launch, and with IDPD_CFG_PLAIN_GRAPHS every step is.
  * Per-particle press and nei_cm_pos are not produced by this path. */
 int idpd_step(idpd_handle* h, int32_t nsteps);
 /* Blocks until the handle's stream is idle; reports device-side errors. */

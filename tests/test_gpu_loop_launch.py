@@ -10,7 +10,7 @@ import pytest
 
 from helpers import mdpd_params, mixed_system
 from implicit_dpd_gb300 import configs
-from implicit_dpd_gb300.abi import CFG_STEP_PER_LAUNCH, FORM_WARREN
+from implicit_dpd_gb300.abi import CFG_PLAIN_GRAPHS, FORM_WARREN
 from implicit_dpd_gb300.engine import Engine, EngineError, derive_params
 
 pytestmark = pytest.mark.gpu
@@ -36,7 +36,7 @@ def _run(flags, skin, sort_period, chunks):
 def test_one_launch_for_k_steps_equals_one_launch_per_step(skin, sort_period):
     chunks = [1, 9, 4, 13]
     a, ra, ta = _run(0, skin, sort_period, chunks)
-    b, rb, tb = _run(CFG_STEP_PER_LAUNCH, skin, sort_period, chunks)
+    b, rb, tb = _run(CFG_PLAIN_GRAPHS, skin, sort_period, chunks)
     for k in ("pos", "vel", "acc", "id", "prop"):
         assert np.array_equal(a[k], b[k]), k
     assert ra == rb and ta == tb == 9 + sum(chunks)
@@ -62,7 +62,7 @@ def test_batched_replicas_one_launch():
         e.close()
         return out
 
-    a, b = run(0), run(CFG_STEP_PER_LAUNCH)
+    a, b = run(0), run(CFG_PLAIN_GRAPHS)
     for x, y in zip(a, b):
         assert np.array_equal(x["pos"], y["pos"]) and np.array_equal(x["vel"], y["vel"])
 
@@ -101,7 +101,7 @@ def test_reaction_in_one_launch_stops_where_the_steps_do():
         e.close()
         return out, t, stopped
 
-    (a, ta, sa), (b, tb, sb) = run(0), run(CFG_STEP_PER_LAUNCH)
+    (a, ta, sa), (b, tb, sb) = run(0), run(CFG_PLAIN_GRAPHS)
     assert sa == sb and ta == tb
     assert len(a["pos"]) == len(b["pos"]) > len(st["pos"])
     for k in ("pos", "vel", "acc", "id", "prop", "amp_id", "unit"):
@@ -127,7 +127,7 @@ def test_observing_steps_between_loop_launches():
         e.close()
         return obs, out
 
-    (oa, a), (ob, b) = run(0), run(CFG_STEP_PER_LAUNCH)
+    (oa, a), (ob, b) = run(0), run(CFG_PLAIN_GRAPHS)
     assert len(oa) == len(ob) > 0
     assert [o["time"] for o in oa] == [o["time"] for o in ob]
     for x, y in zip(oa, ob):
