@@ -101,9 +101,10 @@ struct idpd_handle {
   // asynchronous trajectory frames (idpd_dump_xyz_async): device staging in
   // upload order, its pinned host copy, the copy stream and the writer thread
   cudaStream_t dump_st = nullptr;
-  // idpd_step_host: the copy stream of the positions and its events
+  // idpd_step_host and idpd_download_state: the copy stream of the host
+  // exchange and its events
   cudaStream_t xst = nullptr;
-  cudaEvent_t x_drift = nullptr, x_done = nullptr;
+  cudaEvent_t x_drift = nullptr, x_done = nullptr, x_mid = nullptr;
   cudaEvent_t dump_ready = nullptr, dump_done = nullptr;
   unsigned char* dump_dev = nullptr;
   unsigned char* dump_host = nullptr;
@@ -958,6 +959,7 @@ int idpd_destroy(idpd_handle* h) {
   if (h->cst) cudaStreamDestroy(h->cst);
   if (h->x_drift) cudaEventDestroy(h->x_drift);
   if (h->x_done) cudaEventDestroy(h->x_done);
+  if (h->x_mid) cudaEventDestroy(h->x_mid);
   free_all(h);
   if (h->chem) cudaFree(h->chem);
   if (h->walks) walk_destroy(h->walks);
@@ -1148,6 +1150,47 @@ int idpd_build_topology(idpd_handle* h, int32_t r, int32_t n_amp, int32_t n_core
   return IDPD_OK;
 }
 
+int ensure_xst(idpd_handle* h) {
+  if (h->xst) return IDPD_OK;
+  CK(cudaStreamCreateWithFlags(&h->xst, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&h->x_drift, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->x_done, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->x_mid, cudaEventDisableTiming));
+  return IDPD_OK;
+}
+
+// A storage-order triple (x, y, z arrays) of one replica and where its rows
+// go in upload order (device, managed or host memory; null to skip).
+struct RowTriple {
+  const double *x, *y, *z;
+  double* out;
+  int slot;  // staging slot in h->xfer (3 n doubles each)
+};
+
+// Gathers the triples into upload order on the step's stream and copies the
+// host ones back on the exchange stream, so that each gather after the first
+// runs under the previous copy; the step's stream then waits for the copies.
+int gather_rows_out(idpd_handle* h, const RepDev& R, const RowTriple* f, int nf) {
+  const size_t n = (size_t)R.n;
+  bool copied = false;
+  for (int k = 0; k < nf; k++) {
+    if (!f[k].out) continue;
+    double* view = static_cast<double*>(const_cast<void*>(device_view(f[k].out)));
+    double* tmp = view ? view : h->xfer + 3 * n * f[k].slot;
+    launch_soa_to_aos(f[k].x, f[k].y, f[k].z, h->d.loc, R.row_off, tmp, (int)n, h->st);
+    if (view) continue;
+    CK(cudaEventRecord(h->x_mid, h->st));
+    CK(cudaStreamWaitEvent(h->xst, h->x_mid, 0));
+    CK(cudaMemcpyAsync(f[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->xst));
+    copied = true;
+  }
+  if (copied) {
+    CK(cudaEventRecord(h->x_done, h->xst));
+    CK(cudaStreamWaitEvent(h->st, h->x_done, 0));
+  }
+  return IDPD_OK;
+}
+
 int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, double* acc,
                         uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit) {
   if (!h || r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
@@ -1168,20 +1211,13 @@ int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, dou
   const int n = R.n;
   if (n == 0) return IDPD_OK;
   const DevState& d = h->d;
-  struct F { const double *x, *y, *z; double* out; } f3[3] = {
-      {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
-  int rc = IDPD_OK;
-  for (int k = 0; k < 3; k++) {
-    if (!f3[k].out) continue;
-    // device buffers are written by the kernel directly; host ones through
-    // the staging buffer and one copy
-    double* view = static_cast<double*>(const_cast<void*>(device_view(f3[k].out)));
-    double* tmp = view ? view : h->xfer + 3 * (size_t)n * k;
-    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.loc, R.row_off, tmp, n, h->st);
-    if (view) continue;
-    cudaError_t e = cudaMemcpyAsync(f3[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
-    if (e != cudaSuccess) rc = fail(h, IDPD_ERR_CUDA, "download: %s", cudaGetErrorString(e));
-  }
+  // device buffers are written by the gather directly; host ones through the
+  // staging buffer and one copy each
+  const RowTriple f3[3] = {{d.px, d.py, d.pz, pos, 0}, {d.vx, d.vy, d.vz, vel, 1},
+                           {d.ax, d.ay, d.az, acc, 2}};
+  int rc = ensure_xst(h);
+  if (!rc) rc = gather_rows_out(h, R, f3, 3);
+  if (rc) return rc;
   const uint32_t* uf[4] = {d.id, d.prop, d.amp_id, d.unit};
   uint32_t* uo[4] = {id, prop, amp_id, unit};
   std::vector<uint32_t> orig(n), tmpu(n);
@@ -1511,11 +1547,7 @@ int idpd_step_host(idpd_handle* h, int32_t r, double* pos, double* vel, double* 
     CK(cudaStreamSynchronize(h->st));
     for (uint32_t t : time) observe = observe || (t % (uint32_t)h->obs_period) == 0u;
   }
-  if (!h->xst) {
-    CK(cudaStreamCreateWithFlags(&h->xst, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&h->x_drift, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&h->x_done, cudaEventDisableTiming));
-  }
+  if ((rc = ensure_xst(h))) return rc;
   const RepDev& R = h->reps_h[r];
   const size_t n = (size_t)R.n;
   const DevState& d = h->d;
@@ -1526,17 +1558,18 @@ int idpd_step_host(idpd_handle* h, int32_t r, double* pos, double* vel, double* 
   CK(cudaEventRecord(h->ev1, h->st));
   // positions: gathered to upload order and copied back during the pair passes
   CK(cudaStreamWaitEvent(h->xst, h->x_drift, 0));
-  struct F { const double *x, *y, *z; double* out; } f3[3] = {
-      {d.px, d.py, d.pz, pos}, {d.vx, d.vy, d.vz, vel}, {d.ax, d.ay, d.az, acc}};
-  for (int k = 0; k < 3; k++) {
-    cudaStream_t s = k == 0 ? h->xst : h->st;
-    double* view = static_cast<double*>(const_cast<void*>(device_view(f3[k].out)));
-    double* tmp = view ? view : h->xfer + 3 * n * k;
-    launch_soa_to_aos(f3[k].x, f3[k].y, f3[k].z, d.loc, R.row_off, tmp, (int)n, s);
-    if (!view) CK(cudaMemcpyAsync(f3[k].out, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+  {
+    double* view = static_cast<double*>(const_cast<void*>(device_view(pos)));
+    double* tmp = view ? view : h->xfer;
+    launch_soa_to_aos(d.px, d.py, d.pz, d.loc, R.row_off, tmp, (int)n, h->xst);
+    if (!view) CK(cudaMemcpyAsync(pos, tmp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->xst));
   }
+  // velocities and accelerations after the kick, the second gather under the
+  // first copy; the step's stream then waits for every copy (a reorder
+  // permutes the storage rows: not while they are read)
+  const RowTriple f2[2] = {{d.vx, d.vy, d.vz, vel, 1}, {d.ax, d.ay, d.az, acc, 2}};
+  if ((rc = gather_rows_out(h, R, f2, 2))) return rc;
   CK(cudaEventRecord(h->x_done, h->xst));
-  // a reorder permutes the storage rows: not while the positions are read
   CK(cudaStreamWaitEvent(h->st, h->x_done, 0));
   if (++h->steps_since_sort >= h->sort_period) {
     if ((rc = enqueue_reorder(h))) return rc;

@@ -393,12 +393,16 @@ void launch_aos_to_soa(const double* aos, double* x, double* y, double* z, int n
 // image, as displacement for the kept lists (the delta_sumr of their last
 // rebuild moves back by it), so a host that hands back the positions it read
 // keeps the lists, and one that moves particles far enough triggers a rebuild.
+// One thread per storage row, which reads its upload row's three records
+// (orig maps storage to upload rows): the storage arrays are written in
+// order, and only the 24-byte records are read out of order.
 __global__ void k_set_dynamics(DevState d, const double* pos, const double* vel,
                                const double* acc, int row0, int n, double b0, double b1,
                                double b2, int kept) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const uint32_t i = d.loc[row0 + k];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint32_t i = (uint32_t)(row0 + j);
+  const int k = (int)d.orig[i] - row0;
   const double* p = pos + 3 * (size_t)k;
   const double* v = vel + 3 * (size_t)k;
   const double* a = acc + 3 * (size_t)k;
