@@ -50,6 +50,45 @@ def test_step_host_equals_the_three_calls(skin, sort_period):
     b.close()
 
 
+def _liquid_engine(st, box, skin):
+    e = Engine(sort_period=4)
+    e.set_params(mdpd_params(box, seed=17, time=2))
+    e.upload(st)
+    e.set_tuning(1, skin)
+    return e
+
+
+def test_step_host_with_host_moves():
+    # 233k particles with kept lists and storage reorders every 4 steps; the
+    # host moves particles between steps (small moves kept by the lists, one
+    # large move that forces a rebuild)
+    box = np.array([36.0, 36.0, 36.0])
+    st = configs.liquid(box, 5.0, seed=31)
+    st["id"] = np.arange(len(st["pos"]), dtype=np.uint32)
+    a, b = _liquid_engine(st, box, 0.2), _liquid_engine(st, box, 0.2)
+    pa, va, aa = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    pb, vb, ab = pa.copy(), va.copy(), aa.copy()
+    rng = np.random.default_rng(5)
+    for step in range(10):
+        if step in (4, 7):
+            idx = rng.choice(len(pa), 1000, replace=False)
+            shift = rng.uniform(-0.02, 0.02, size=(1000, 3))
+            if step == 7:
+                shift[0] = (0.3, 0.0, 0.0)  # beyond half the skin
+            for p_ in (pa, pb):
+                p_[idx] = np.mod(p_[idx] + shift, box)
+        a.set_dynamics(pa, va, aa)
+        a.step(1)
+        a.download_dynamics(pa, va, aa)
+        b.step_host(pb, vb, ab)
+        for x, y, name in ((pa, pb, "pos"), (va, vb, "vel"), (aa, ab, "acc")):
+            assert np.array_equal(x, y), f"{name} differs at step {step}"
+        assert a.list_rebuilds() == b.list_rebuilds(), step
+    assert b.list_rebuilds() >= 3
+    a.close()
+    b.close()
+
+
 def test_step_host_on_a_batched_handle():
     # replica 1 is exchanged; both replicas step
     box = np.array([8.0, 8.0, 8.0])
