@@ -13,8 +13,10 @@ import json
 import math
 import os
 
-DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (2, 0.15), (2, 0.2),
-                   (2, 0.3))
+# (reach, skin); liquids, which diffuse fast, do best near skin 0.35 (fewer
+# rebuilds for longer kept lists), membranes near 0.15 - 0.2
+DEFAULT_CHOICES = ((1, 0.0), (2, 0.0), (1, 0.1), (1, 0.15), (1, 0.2), (1, 0.25), (1, 0.3),
+                   (1, 0.35), (2, 0.15), (2, 0.2), (2, 0.3))
 # (lanes per particle, row blocks per CTA) of the force pass; the first is the default
 SHAPES = ((16, 1), (8, 1), (32, 1), (8, 2), (16, 2), (4, 1), (4, 2))
 # lanes per particle of the density pass over kept lists; the first is the default
