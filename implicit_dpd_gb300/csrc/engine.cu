@@ -1068,10 +1068,19 @@ int idpd_set_dynamics(idpd_handle* h, int32_t r, const double* pos, const double
   if (!h || r < 0 || r >= h->R || !pos || !vel || !acc)
     return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
   if (!h->on_device || h->layout_dirty) {
-    // not on the device yet: the rows wait in the staging buffers
+    // not on the device yet: the rows wait in the staging buffers (caller
+    // buffers in device memory are copied over first, never read by the host)
     Staged& s = h->staged[r];
     const size_t n = (size_t)h->n[r];
     if (s.pos.size() != 3 * n) return fail(h, IDPD_ERR_STATE, "upload the state first");
+    std::vector<double> tmp[3];
+    const double** src[3] = {&pos, &vel, &acc};
+    for (int k = 0; k < 3; k++)
+      if (device_view(*src[k])) {
+        tmp[k].resize(3 * n);
+        CK(cudaMemcpy(tmp[k].data(), *src[k], sizeof(double) * 3 * n, cudaMemcpyDefault));
+        *src[k] = tmp[k].data();
+      }
     const idpd_params& p = h->params[r];
     for (size_t i = 0; i < 3 * n; i++)
       if (!std::isfinite(pos[i]) || !std::isfinite(vel[i]) || !std::isfinite(acc[i]) ||
@@ -1195,15 +1204,21 @@ int idpd_download_state(idpd_handle* h, int32_t r, double* pos, double* vel, dou
                         uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit) {
   if (!h || r < 0 || r >= h->R) return fail(h, IDPD_ERR_INVALID_ARG, "bad argument");
   if (!h->on_device || h->layout_dirty) {
+    // the staged rows; caller buffers in device memory are written by copies
     const Staged& s = h->staged[r];
-    const int n = h->n[r];
-    if (pos) std::copy(s.pos.begin(), s.pos.begin() + 3 * n, pos);
-    if (vel) std::copy(s.vel.begin(), s.vel.begin() + 3 * n, vel);
-    if (acc) std::copy(s.acc.begin(), s.acc.begin() + 3 * n, acc);
-    if (id) std::copy(s.id.begin(), s.id.begin() + n, id);
-    if (prop) std::copy(s.prop.begin(), s.prop.begin() + n, prop);
-    if (amp_id) std::copy(s.amp_id.begin(), s.amp_id.begin() + n, amp_id);
-    if (unit) std::copy(s.unit.begin(), s.unit.begin() + n, unit);
+    const size_t n = (size_t)h->n[r];
+    struct Out { void* dst; const void* src; size_t bytes; } outs[7] = {
+        {pos, s.pos.data(), sizeof(double) * 3 * n}, {vel, s.vel.data(), sizeof(double) * 3 * n},
+        {acc, s.acc.data(), sizeof(double) * 3 * n}, {id, s.id.data(), sizeof(uint32_t) * n},
+        {prop, s.prop.data(), sizeof(uint32_t) * n}, {amp_id, s.amp_id.data(), sizeof(uint32_t) * n},
+        {unit, s.unit.data(), sizeof(uint32_t) * n}};
+    for (const Out& o : outs) {
+      if (!o.dst || o.bytes == 0) continue;
+      if (device_view(o.dst))
+        CK(cudaMemcpy(o.dst, o.src, o.bytes, cudaMemcpyDefault));
+      else
+        std::memcpy(o.dst, o.src, o.bytes);
+    }
     return IDPD_OK;
   }
   cudaSetDevice(h->device);

@@ -145,11 +145,15 @@ int idpd_num_particles(const idpd_handle* h, int32_t replica, int32_t* n);
  * an uploaded replica, in upload order, keeping ids, properties and the
  * topology. Positions outside [0, box] or non-finite values are rejected by
  * the device and reported by the next call (before the first pass after an
- * upload, they are checked on the host and the staged rows are replaced). */
+ * upload, they are checked on the host and the staged rows are replaced).
+ * The arrays may also lie in device or managed memory: the kernels then read
+ * them where they lie (before the first pass, they are copied to the host). */
 int idpd_set_dynamics(idpd_handle* h, int32_t replica, const double* pos, const double* vel,
                       const double* acc);
 /* Any pointer may be NULL to skip that field. Rows come back in the order
- * they were uploaded (new particles from chemistry appended). */
+ * they were uploaded (new particles from chemistry appended). Buffers in
+ * device or managed memory are written there by the kernels (or by copies,
+ * before the first pass). */
 int idpd_download_state(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc,
                         uint32_t* id, uint32_t* prop, uint32_t* amp_id, uint32_t* unit);
 /* One MD step on host arrays: the reference's loop body (src/main.cpp:166-209)
@@ -160,7 +164,8 @@ int idpd_download_state(idpd_handle* h, int32_t replica, double* pos, double* ve
  * that of the three calls bit for bit; the positions, final after the drift,
  * are copied back while the pair passes run, and the call synchronises once.
  * Not with the reaction enabled (IDPD_ERR_STATE: the reaction can add
- * particles during the step). */
+ * particles during the step). The arrays may lie in device or managed memory,
+ * as for idpd_set_dynamics and idpd_download_state. */
 int idpd_step_host(idpd_handle* h, int32_t replica, double* pos, double* vel, double* acc);
 /* Derived per-particle fields: density[3] (FPDPD::density), press[3]
  * (FPDPD::press), nei_cm_pos[2][3] (FPDPD::nei_cm_pos), delta_sumr[3]. */
