@@ -1835,45 +1835,45 @@ int idpd_profile_step(idpd_handle* h, char* names, size_t names_len, float* ms, 
   return check_device_error(h);
 }
 
+// Saru test draws on the device: the keys in, the draws out. One device
+// block holds keys and draws and is freed on every path.
+static int saru_draws(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
+                      int32_t draws, uint32_t* out_u, float* out_n) {
+  idpd_handle* h = nullptr;
+  const size_t nk = (size_t)n, nd = out_u ? nk * (size_t)draws : nk;
+  uint32_t* buf = nullptr;
+  CK(cudaMalloc((void**)&buf, 4 * (3 * nk + nd)));
+  cudaError_t e = cudaSuccess;
+  const uint32_t* src[3] = {s1, s2, s3};
+  for (int k = 0; k < 3 && e == cudaSuccess; k++)
+    e = cudaMemcpy(buf + k * nk, src[k], 4 * nk, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    uint32_t* dout = buf + 3 * nk;
+    launch_saru_test(n, buf, buf + nk, buf + 2 * nk, out_u ? draws : 0, out_u ? dout : nullptr,
+                     out_u ? nullptr : reinterpret_cast<float*>(dout), 0);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpy(out_u ? (void*)out_u : (void*)out_n, dout, 4 * nd, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(nullptr, IDPD_ERR_CUDA, "saru draws: %s", cudaGetErrorString(e));
+  return IDPD_OK;
+}
+
 int idpd_saru_u32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
                   int32_t draws, uint32_t* out) {
-  idpd_handle* h = nullptr;
   if (n < 0 || draws < 0 || (n > 0 && (!s1 || !s2 || !s3 || !out)))
     return fail(nullptr, IDPD_ERR_INVALID_ARG, "bad argument");
   if (n == 0 || draws == 0) return IDPD_OK;
-  uint32_t *d1, *d2, *d3, *dout;
-  CK(cudaMalloc((void**)&d1, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&d2, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&d3, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&dout, 4 * (size_t)n * draws));
-  CK(cudaMemcpy(d1, s1, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d2, s2, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d3, s3, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  launch_saru_test(n, d1, d2, d3, draws, dout, nullptr, 0);
-  CK(cudaMemcpy(out, dout, 4 * (size_t)n * draws, cudaMemcpyDeviceToHost));
-  cudaFree(d1); cudaFree(d2); cudaFree(d3); cudaFree(dout);
-  return IDPD_OK;
+  return saru_draws(n, s1, s2, s3, draws, out, nullptr);
 }
 
 int idpd_saru_nrml_f32(int32_t n, const uint32_t* s1, const uint32_t* s2, const uint32_t* s3,
                        float* out) {
-  idpd_handle* h = nullptr;
   if (n < 0 || (n > 0 && (!s1 || !s2 || !s3 || !out)))
     return fail(nullptr, IDPD_ERR_INVALID_ARG, "bad argument");
   if (n == 0) return IDPD_OK;
-  uint32_t *d1, *d2, *d3;
-  float* dout;
-  CK(cudaMalloc((void**)&d1, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&d2, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&d3, 4 * (size_t)n));
-  CK(cudaMalloc((void**)&dout, 4 * (size_t)n));
-  CK(cudaMemcpy(d1, s1, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d2, s2, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d3, s3, 4 * (size_t)n, cudaMemcpyHostToDevice));
-  launch_saru_test(n, d1, d2, d3, 0, nullptr, dout, 0);
-  CK(cudaMemcpy(out, dout, 4 * (size_t)n, cudaMemcpyDeviceToHost));
-  cudaFree(d1); cudaFree(d2); cudaFree(d3); cudaFree(dout);
-  return IDPD_OK;
+  return saru_draws(n, s1, s2, s3, 0, nullptr, out);
 }
 
 int idpd_cell_order(idpd_handle* h, int32_t r, uint32_t* cell_of_row, uint32_t* perm_out) {
