@@ -430,20 +430,55 @@ def reaction_bench(tune, steps=100, equil=2000, device=0):
                            "tail bead (Saru(id, step, seed) draw, bit-exact decisions)"}
 
 
-def liquid_bench(steps=200, equil=300, device=0):
+def liquid_workload():
     """The 10^6-particle MDPD liquid: 55^3 box at density 6 (998,250
     particles), Warren form A = -40, B = 25, r_d = 0.75, sigma 3, dt 0.005,
-    uniform random start. The FP32 engine (tuned by the package's tuner) against
-    the plain FP64 kernels of the same step, with the measured force error."""
-    from implicit_dpd_gb300.abi import CFG_FP64_KEPT, CFG_FP64_PAIRS, FORM_WARREN
-    from implicit_dpd_gb300.engine import Engine, derive_params
+    uniform random start."""
+    from implicit_dpd_gb300.abi import FORM_WARREN
+    from implicit_dpd_gb300.engine import derive_params
 
     box = np.array([55.0, 55.0, 55.0])
     st = configs.liquid(box, 6.0, seed=12350)
-    n = len(st["pos"])
     p = derive_params(configs.run_param(box, dt=0.005, cf_r=3.0))
     p.seed, p.time, p.form = 2468, 1, FORM_WARREN
     p.warren_a, p.warren_b, p.warren_rd = -40.0, 25.0, 0.75
+    return box, st, p
+
+
+# (reach, skin, lanes, blocks, pass-1 lanes) the package's tuner picks for the liquid
+LIQUID_TUNE = (1, 0.3, 4, 2, 4)
+
+
+def run_liquid_case(equil, device=0):
+    """The liquid from its uniform start at its tuned shape: `equil` graph
+    steps, then 12 more (kept-list steps, for launch lists of the liquid)."""
+    from implicit_dpd_gb300.engine import Engine
+
+    box, st, p = liquid_workload()
+    e = Engine(flags=GRAPH_FLAGS, sort_period=100, device=device)
+    e.set_params(p)
+    e.upload(st)
+    reach, skin, lanes, blocks, dl = LIQUID_TUNE
+    e.set_tuning(reach, skin, lanes=lanes, blocks=blocks, dens_lanes=dl)
+    e.step(equil)
+    e.step(12)
+    e.sync()
+    print(json.dumps({"liquid_case": "mdpd_liquid_1m", "n_particles": len(st["pos"]),
+                      "steps": equil + 12, "rebuilds": e.list_rebuilds(),
+                      "tuning": dict(zip(("reach", "skin", "lanes", "blocks", "dens_lanes"),
+                                         LIQUID_TUNE))}), flush=True)
+    e.close()
+
+
+def liquid_bench(steps=200, equil=300, device=0):
+    """The 10^6-particle MDPD liquid (liquid_workload). The FP32 engine (tuned
+    by the package's tuner) against the plain FP64 kernels of the same step,
+    with the measured force error."""
+    from implicit_dpd_gb300.abi import CFG_FP64_KEPT, CFG_FP64_PAIRS
+    from implicit_dpd_gb300.engine import Engine
+
+    box, st, p = liquid_workload()
+    n = len(st["pos"])
 
     def engine(flags=0, state=st):
         e = Engine(flags=flags, sort_period=100, device=device)
@@ -964,6 +999,9 @@ def main():
                     help="one graph launch per step and no conditional nodes (for ncu)")
     ap.add_argument("--kernel-case", default=None,
                     help="load a saved state and run three graph steps (profiling case)")
+    ap.add_argument("--liquid-case", type=int, default=None, metavar="STEPS",
+                    help="the MDPD liquid at its tuned shape: STEPS graph steps, then 12 "
+                         "(profiling case)")
     ap.add_argument("--reach", type=int, default=0,
                     help="cell reach (1 or 2) instead of the autotuned one")
     ap.add_argument("--skin", type=float, default=0.0,
@@ -982,6 +1020,9 @@ def main():
     if args.kernel_case:
         run_kernel_case(args.kernel_case, local_rank, args.reach,
                         args.skin if args.reach else None)
+        return
+    if args.liquid_case is not None:
+        run_liquid_case(args.liquid_case, local_rank)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
