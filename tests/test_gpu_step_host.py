@@ -50,6 +50,34 @@ def test_step_host_equals_the_three_calls(skin, sort_period):
     b.close()
 
 
+def test_step_host_with_observations():
+    # observing steps go through the observation kernels in both forms; the
+    # states and the drained records are the same bit for bit
+    box, st, n_amp = mixed_system(seed=24)
+    p = mdpd_params(box, time=4)
+    a = _engine(p, st, n_amp, 0.2, 3)
+    b = _engine(p, st, n_amp, 0.2, 3)
+    for e in (a, b):
+        e.set_observe(2)
+    pa, va, aa = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    pb, vb, ab = pa.copy(), va.copy(), aa.copy()
+    for step in range(7):
+        a.set_dynamics(pa, va, aa)
+        a.step(1)
+        a.download_dynamics(pa, va, aa)
+        b.step_host(pb, vb, ab)
+        for x, y, name in ((pa, pb, "pos"), (va, vb, "vel"), (aa, ab, "acc")):
+            assert np.array_equal(x, y), f"{name} differs at step {step}"
+    oa, ob = a.observations(), b.observations()
+    assert len(oa) == len(ob) >= 3
+    for x, y in zip(oa, ob):
+        assert x["time"] == y["time"] and x["time"] % 2 == 0
+        for k in ("kin_temp", "pressure", "diffusion"):
+            assert np.array_equal(x[k], y[k]), k
+    a.close()
+    b.close()
+
+
 def test_step_host_with_device_buffers():
     # device buffers are read and written by the kernels where they lie; the
     # result equals that of page-locked or pageable host arrays bit for bit
