@@ -78,6 +78,33 @@ def test_step_host_with_observations():
     b.close()
 
 
+def test_step_host_with_the_precursor_conversion():
+    # the conversion changes properties on the device during the step; the
+    # host exchange carries pos/vel/acc only, and both forms convert the same
+    # particles
+    from implicit_dpd_gb300.abi import HYPHIL, HYPHOB, SOLVENT, precursor_threshold
+    box, st, n_amp = mixed_system(seed=12)
+    p = mdpd_params(box, time=300)
+    thr = precursor_threshold(0.05)
+    a = _engine(p, st, n_amp, 0.2, 4)
+    b = _engine(p, st, n_amp, 0.2, 4)
+    for e in (a, b):
+        e.set_precursor(SOLVENT, HYPHOB, HYPHIL, thr, 4242)
+    pa, va, aa = (np.ascontiguousarray(st[k], np.float64).copy() for k in ("pos", "vel", "acc"))
+    pb, vb, ab = pa.copy(), va.copy(), aa.copy()
+    for step in range(6):
+        a.set_dynamics(pa, va, aa)
+        a.step(1)
+        a.download_dynamics(pa, va, aa)
+        b.step_host(pb, vb, ab)
+        for x, y, name in ((pa, pb, "pos"), (va, vb, "vel"), (aa, ab, "acc")):
+            assert np.array_equal(x, y), f"{name} differs at step {step}"
+    assert a.precursor_count() == b.precursor_count() > 20
+    assert np.array_equal(a.download()["prop"], b.download()["prop"])
+    a.close()
+    b.close()
+
+
 def test_step_host_with_device_buffers():
     # device buffers are read and written by the kernels where they lie; the
     # result equals that of page-locked or pageable host arrays bit for bit
